@@ -1,0 +1,271 @@
+/*
+ * ns3d_capi.h -- C-ABI of the NS3D steady staggered-grid Navier-Stokes
+ * permeability solver (GB300 / sm_103a implementation).
+ *
+ * The reference solver (jerome-lux/NS3D) has no plugin API: its seam is the
+ * C++ class NavierStokesBase (src/NSBase.h:63-594) driven by the four
+ * XSOLVER::Solve(NavierStokesBase&) drivers and selected in main
+ * (src/navierstokes3D.cxx:516-542).  Every entry point below replaces one
+ * piece of that surface; the reference interface it stands for is cited on
+ * each declaration.
+ *
+ * Conventions
+ *  - Plain C types only; the caller owns every host buffer, the library owns
+ *    device memory.
+ *  - Every function returns an int status: NS3D_OK (0) or a negative API
+ *    error.  Linear-solver outcomes use the numeric values of Eigen's
+ *    ComputationInfo, which the reference prints as "(status N)" in its INFO
+ *    log: Success 0, NumericalIssue 1, NoConvergence 2, InvalidInput 3.
+ *  - No C++ exception crosses the ABI.  ns3d_last_error() returns the text of
+ *    the last error raised on the calling thread.
+ *  - A handle is used by one host thread at a time; separate handles may run
+ *    concurrently (each owns its own CUDA stream).
+ *  - Index maps are int32 in C order (i = x outermost, k = z fastest), the
+ *    layout of the reference's blitz::Array<int,3> (src/NSBase.h:90-93), in
+ *    the rotated/padded frame in which the flow runs along x.
+ *
+ * The CPU oracle under oracle/ implements this same header, so the two
+ * libraries can be swapped for A/B runs.
+ */
+#ifndef NS3D_CAPI_H
+#define NS3D_CAPI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#if defined(_WIN32)
+#define NS3D_API __declspec(dllexport)
+#else
+#define NS3D_API __attribute__((visibility("default")))
+#endif
+
+#define NS3D_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    NS3D_OK = 0,
+    /* linear-solver statuses (Eigen ComputationInfo values) */
+    NS3D_SUCCESS = 0,
+    NS3D_NUMERICAL_ISSUE = 1,
+    NS3D_NO_CONVERGENCE = 2,
+    NS3D_INVALID_INPUT = 3,
+    /* API errors */
+    NS3D_ERR_ARG = -1,         /* bad argument (NULL pointer, bad size, bad key value) */
+    NS3D_ERR_OOM = -2,         /* device or host allocation failed */
+    NS3D_ERR_CUDA = -3,        /* a CUDA call failed */
+    NS3D_ERR_IO = -4,          /* file could not be opened / read / written */
+    NS3D_ERR_PARSE = -5,       /* malformed ini or .vti content */
+    NS3D_ERR_STATE = -6,       /* call out of order (e.g. fields before open) */
+    NS3D_ERR_TIMEOUT = -7,     /* a bounded device wait ran out */
+    NS3D_ERR_UNSUPPORTED = -8  /* feature not available in this build */
+};
+
+/* outer-loop algorithm, src/navierstokes3D.cxx:522-542 */
+enum { NS3D_SIMPLEC = 0, NS3D_SIMPLER = 1, NS3D_SIMPLERR = 2, NS3D_IDEAL = 3 };
+
+/* arithmetic of the inner solves */
+enum { NS3D_FP64 = 0, NS3D_MIXED = 1 };
+
+/* systems addressed by the step-level entry points */
+enum { NS3D_SYS_U = 0, NS3D_SYS_V = 1, NS3D_SYS_W = 2, NS3D_SYS_P = 3 };
+
+/*
+ * Solver parameters: the ini keys of the reference (InputParams,
+ * src/navierstokes3D.cxx:162-201), same names, meaning and defaults.
+ * method/precision are integers (see the enums above).
+ */
+typedef struct ns3d_params {
+    double dx, dy, dz;             /* grid spacing (m); dy,dz <= 0 mean "same as dx" */
+    double mu, rho;                /* viscosity (Pa.s), density (kg/m^3) */
+    double p0, gradp;              /* inlet pressure (Pa), imposed gradient (Pa/m) */
+    double alpha, beta;            /* velocity / pressure relaxation */
+    double vsolvertol, psolvertol, pcsolvertol;
+    double simpletol, deltaRMR;
+    int32_t maxitsolver, maxitSIMPLE, N1, N2, save_step;
+    int32_t porevalue, direction, border;
+    int32_t method, precision;
+} ns3d_params;
+
+/* grid and system sizes after rotation and border padding */
+typedef struct ns3d_sizes {
+    int32_t nx, ny, nz;
+    int32_t np, nu, nv, nw;
+    int32_t reserved;
+} ns3d_sizes;
+
+/* diagnostics of the last outer iteration and of the whole solve */
+typedef struct ns3d_result {
+    double K, Q, v_moy, RMR;
+    double normdiv, reldiv, velocityNorm, maxdiv, MaxDeltaV;
+    double p_inlet, p_outlet, p0, p1;
+    double alpha, beta;
+    double pcmax, pcmin, pcnorm;
+    double seconds;                /* wall time of ns3d_solve */
+    int32_t iterations;            /* loop index at exit ("terminated in N iteration") */
+    int32_t converged;             /* CheckConvergence returned true */
+    int32_t it_u, it_v, it_w, it_p;/* iterations() of the last u/v/w/p solve */
+    int64_t krylov_iterations;     /* BiCGSTAB iterations summed over every solve */
+    int64_t krylov_rows;           /* sum over solves of iterations x rows */
+} ns3d_result;
+
+/* outcome of one BiCGSTAB solve (Eigen iterations()/error()/info()) */
+typedef struct ns3d_solve_info {
+    int32_t iterations;
+    int32_t info;
+    double error;
+} ns3d_solve_info;
+
+typedef struct ns3d_handle ns3d_handle;
+
+/* ---- library ----------------------------------------------------------- */
+NS3D_API int ns3d_abi_version(void);
+/* "gb300" for the CUDA library, "oracle" for the CPU restatement */
+NS3D_API const char *ns3d_backend_name(void);
+NS3D_API const char *ns3d_last_error(void);
+
+/* Fill *p with the reference defaults, src/navierstokes3D.cxx:162-201. */
+NS3D_API void ns3d_params_default(ns3d_params *p);
+
+/* ---- geometry ---------------------------------------------------------- */
+/*
+ * Build a solver instance from a raw voxel image.
+ * raw: nx*ny*nz bytes in VTK order (x fastest), as read from the .vti file
+ *      (readvtkfile_uint8, src/vtkio.cxx:96-150): a voxel equal to
+ *      params->porevalue is fluid.
+ * The image is binarized, rotated so the flow runs along x
+ * (NavierStokesBase::Rotation, src/NSBase.cxx:2451-2492), padded along x
+ * (AddBorder, src/NSBase.cxx:2425-2448) and indexed
+ * (InitIndexArrays, src/NSBase.cxx:2495-2573); p1 and the relaxation
+ * constants are set as in the constructor (src/NSBase.cxx:155-179).
+ * Replaces NavierStokesBase::NavierStokesBase (src/NSBase.cxx:50-194).
+ */
+NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw,
+                       int32_t nx, int32_t ny, int32_t nz, ns3d_handle **out);
+
+/* Sizes after rotation/padding and the counts np/nu/nv/nw
+ * (NavierStokesBase members nx..nw, src/NSBase.h:77). */
+NS3D_API int ns3d_get_sizes(const ns3d_handle *h, ns3d_sizes *s);
+
+/* Copy the index maps (pindex, uindex, vindex, windex; src/NSBase.h:90-93).
+ * Shapes: p,v,w nx*ny*nz; u (nx+1)*ny*nz.  Any pointer may be NULL. */
+NS3D_API int ns3d_get_index_arrays(ns3d_handle *h, int32_t *pindex, int32_t *uindex,
+                                   int32_t *vindex, int32_t *windex);
+
+/* ---- fields ------------------------------------------------------------ */
+/*
+ * Initial fields, image-shaped in the rotated frame (p: nx*ny*nz,
+ * u: (nx+1)*ny*nz, v,w: nx*ny*nz).  NULL keeps the default: the linear
+ * pressure profile p0 + (p1-p0)(i+1)/nx (Initpvector, src/NSBase.cxx:2645-2690)
+ * and zero velocity (InitVelocity, src/NSBase.cxx:2575-2642).
+ */
+NS3D_API int ns3d_set_initial_fields(ns3d_handle *h, const double *p_img, const double *u_img,
+                                     const double *v_img, const double *w_img);
+
+/* Compacted fields (lengths np, nu, nv, nw).  Any pointer may be NULL. */
+NS3D_API int ns3d_get_fields(ns3d_handle *h, double *p, double *u, double *v, double *w);
+NS3D_API int ns3d_set_fields(ns3d_handle *h, const double *p, const double *u,
+                             const double *v, const double *w);
+
+/*
+ * Image-shaped fields as written by FieldsToImage (src/NSBase.cxx:330-476):
+ * p, v, w: nx*ny*nz; u: (nx+1)*ny*nz; vavg: 3*nx*ny*nz interleaved
+ * (face-averaged cell velocity).  Zeros where no node exists.  C order.
+ */
+NS3D_API int ns3d_get_field_images(ns3d_handle *h, double *p_img, double *u_img, double *v_img,
+                                   double *w_img, double *vavg_img);
+
+/* ---- logs and outputs -------------------------------------------------- */
+/*
+ * Write the INFO / RES logs (INFO-<dir>-<stem>.log, RES-<dir>-<stem>.csv,
+ * src/NSBase.cxx:107-123) and, for the CUDA library, the field snapshots
+ * and final .vti files (<stem>-SAVE-k.vti, P-/V-/Vx-/Vy-/Vz-<dir>-<stem>.vti)
+ * into directory `dir`.  dir == NULL disables all file output.
+ * write_fields = 0 keeps the logs but skips the .vti files.
+ */
+NS3D_API int ns3d_set_output(ns3d_handle *h, const char *dir, const char *stem,
+                             int32_t write_fields);
+
+/* ---- solve ------------------------------------------------------------- */
+/*
+ * Run the outer loop selected by params->method (SIMPLECSOLVER::Solve
+ * src/SIMPLEC.cxx:73-232, SIMPLERSOLVER::Solve src/SIMPLER.cxx:75-270,
+ * SIMPLERRSOLVER::Solve src/SIMPLERR.cxx:75-280, IDEALSOLVER::Solve
+ * src/IDEAL.cxx:75-281) from the current initial fields.
+ */
+NS3D_API int ns3d_solve(ns3d_handle *h);
+NS3D_API int ns3d_get_result(const ns3d_handle *h, ns3d_result *r);
+
+/* ---- step-level entry points (one reference method each) --------------- */
+/* AssembleAllMomentum on the current u,v,w (src/NSBase.cxx:853-884). */
+NS3D_API int ns3d_assemble_momentum(ns3d_handle *h);
+/* AssemblePressureCorrectionSIMPLEC (simplec=1, src/NSBase.cxx:612-732) or
+ * ...SIMPLE (simplec=0, src/NSBase.cxx:734-851) on the current fields. */
+NS3D_API int ns3d_assemble_pressure_correction(ns3d_handle *h, int32_t simplec);
+/* Compute_{u,v,w}_hat (src/NSBase.cxx:1548-1755) with uc = u_old = current
+ * velocity, then AssemblePressure (src/NSBase.cxx:478-610). */
+NS3D_API int ns3d_assemble_pressure(ns3d_handle *h, int32_t relax);
+/*
+ * Copy the last assembled system `sys` (NS3D_SYS_*): coef is 7*n doubles,
+ * slot-major [P,W,E,S,N,B,T][n] (missing entries are 0); nbr is 6*n int32
+ * [W,E,S,N,B,T][n] (-1 = no entry); rhs n doubles; rowsum n doubles
+ * (uA.row(r).sum(), momentum systems only).  Any pointer may be NULL.
+ */
+NS3D_API int ns3d_get_system(ns3d_handle *h, int32_t sys, double *coef, int32_t *nbr,
+                             double *rhs, double *rowsum);
+/*
+ * BiCGSTAB with Jacobi preconditioning on the assembled system `sys`
+ * (Eigen::BiCGSTAB::solveWithGuess as used at src/NSBase.cxx:1799,2343):
+ * x holds the guess on entry and the solution on exit; rhs NULL uses the
+ * system's assembled right-hand side.
+ */
+NS3D_API int ns3d_solve_system(ns3d_handle *h, int32_t sys, const double *rhs, double *x,
+                               double tol, int32_t maxit, ns3d_solve_info *info);
+
+NS3D_API int ns3d_close(ns3d_handle *h);
+
+/* ---- host utilities (CUDA library only; no device work) ----------------- */
+/*
+ * Parse an ini file like ReadInput (src/navierstokes3D.cxx:266-463): same
+ * keys, defaults, validation and messages (written to stderr).  The file
+ * keys (input, pressurefield, vxfield, vyfield, vzfield) are copied into the
+ * caller's buffers of `cap` bytes each (any may be NULL).  One key is added
+ * to the reference's set: precision = FP64 | MIXED.
+ * Returns NS3D_OK, NS3D_ERR_IO (cannot open) or NS3D_ERR_PARSE (fatal error).
+ */
+NS3D_API int ns3d_ini_read(const char *path, ns3d_params *p, char *input, char *pressurefield, char *vxfield,
+                           char *vyfield, char *vzfield, size_t cap);
+/*
+ * Read a .vti (VTK XML ImageData, appended/inline, raw/base64, zlib or not)
+ * or legacy .vtk STRUCTURED_POINTS file (readvtkfile_uint8 /
+ * readvtkfile_double, src/vtkio.cxx:38-150).  dims receives nx, ny, nz and
+ * ncomp the component count; values are returned in file order (x fastest).
+ * With buf == NULL only the sizes are returned.  cap is the buffer length in
+ * elements.
+ */
+NS3D_API int ns3d_vti_read_u8(const char *path, uint8_t *buf, size_t cap, int32_t dims[3]);
+NS3D_API int ns3d_vti_read_f64(const char *path, double *buf, size_t cap, int32_t dims[3], int32_t *ncomp);
+/* Write nx*ny*nz*ncomp doubles given in C order (x slowest) as a Float64
+ * zlib-compressed appended .vti (writeScalarImage / writeVectorImage,
+ * src/vtkio.cxx:161-246). */
+NS3D_API int ns3d_vti_write_f64(const char *path, const double *data, int32_t nx, int32_t ny, int32_t nz,
+                                int32_t ncomp);
+/* Write a binary uint8 image given in file order (x fastest)
+ * (writeBinaryImage, src/vtkio.cxx:254-291). */
+NS3D_API int ns3d_vti_write_u8(const char *path, const uint8_t *data, int32_t nx, int32_t ny, int32_t nz);
+/*
+ * The NS3D program: read the ini, the image and the restart fields, solve,
+ * write INFO/RES logs and the .vti fields into out_dir (NULL = current
+ * directory) -- main, src/navierstokes3D.cxx:480-545.  If result is not NULL
+ * it receives the final diagnostics.
+ */
+NS3D_API int ns3d_run_ini(const char *ini_path, const char *out_dir, ns3d_result *result);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NS3D_CAPI_H */

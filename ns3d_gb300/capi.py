@@ -1,0 +1,228 @@
+"""ctypes binding of the NS3D C-ABI (include/ns3d_capi.h).
+
+The same binding drives any library that implements the header: the CUDA
+library built in this package and, in the tests, the CPU oracle.  This is the
+binding a Python caller of the reference's solver path would add; the cgo and
+C++ forms are shown in INTEGRATION.md.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+NS3D_OK = 0
+SUCCESS, NUMERICAL_ISSUE, NO_CONVERGENCE, INVALID_INPUT = 0, 1, 2, 3
+ERR_ARG, ERR_OOM, ERR_CUDA, ERR_IO, ERR_PARSE, ERR_STATE, ERR_TIMEOUT, ERR_UNSUPPORTED = range(-1, -9, -1)
+SIMPLEC, SIMPLER, SIMPLERR, IDEAL = 0, 1, 2, 3
+FP64, MIXED = 0, 1
+SYS_U, SYS_V, SYS_W, SYS_P = 0, 1, 2, 3
+METHODS = {"SIMPLEC": SIMPLEC, "SIMPLER": SIMPLER, "SIMPLERR": SIMPLERR, "IDEAL": IDEAL}
+
+
+class Params(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "dx", "dy", "dz", "mu", "rho", "p0", "gradp", "alpha", "beta",
+        "vsolvertol", "psolvertol", "pcsolvertol", "simpletol", "deltaRMR")] + \
+        [(n, C.c_int32) for n in (
+            "maxitsolver", "maxitSIMPLE", "N1", "N2", "save_step",
+            "porevalue", "direction", "border", "method", "precision")]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class Sizes(C.Structure):
+    _fields_ = [(n, C.c_int32) for n in ("nx", "ny", "nz", "np", "nu", "nv", "nw", "reserved")]
+
+
+class Result(C.Structure):
+    _fields_ = [(n, C.c_double) for n in (
+        "K", "Q", "v_moy", "RMR", "normdiv", "reldiv", "velocityNorm", "maxdiv", "MaxDeltaV",
+        "p_inlet", "p_outlet", "p0", "p1", "alpha", "beta", "pcmax", "pcmin", "pcnorm", "seconds")] + \
+        [(n, C.c_int32) for n in ("iterations", "converged", "it_u", "it_v", "it_w", "it_p")] + \
+        [("krylov_iterations", C.c_int64), ("krylov_rows", C.c_int64)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("info", C.c_int32), ("error", C.c_double)]
+
+
+_P = C.POINTER
+_d = _P(C.c_double)
+_i32 = _P(C.c_int32)
+
+
+class NS3DError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("ns3d error %d: %s" % (code, msg))
+        self.code = code
+
+
+def _declare(lib):
+    sig = {
+        "ns3d_abi_version": (C.c_int, []),
+        "ns3d_backend_name": (C.c_char_p, []),
+        "ns3d_last_error": (C.c_char_p, []),
+        "ns3d_params_default": (None, [_P(Params)]),
+        "ns3d_open": (C.c_int, [_P(Params), _P(C.c_uint8), C.c_int32, C.c_int32, C.c_int32, _P(C.c_void_p)]),
+        "ns3d_get_sizes": (C.c_int, [C.c_void_p, _P(Sizes)]),
+        "ns3d_get_index_arrays": (C.c_int, [C.c_void_p, _i32, _i32, _i32, _i32]),
+        "ns3d_set_initial_fields": (C.c_int, [C.c_void_p, _d, _d, _d, _d]),
+        "ns3d_get_fields": (C.c_int, [C.c_void_p, _d, _d, _d, _d]),
+        "ns3d_set_fields": (C.c_int, [C.c_void_p, _d, _d, _d, _d]),
+        "ns3d_get_field_images": (C.c_int, [C.c_void_p, _d, _d, _d, _d, _d]),
+        "ns3d_set_output": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_int32]),
+        "ns3d_solve": (C.c_int, [C.c_void_p]),
+        "ns3d_get_result": (C.c_int, [C.c_void_p, _P(Result)]),
+        "ns3d_assemble_momentum": (C.c_int, [C.c_void_p]),
+        "ns3d_assemble_pressure_correction": (C.c_int, [C.c_void_p, C.c_int32]),
+        "ns3d_assemble_pressure": (C.c_int, [C.c_void_p, C.c_int32]),
+        "ns3d_get_system": (C.c_int, [C.c_void_p, C.c_int32, _d, _i32, _d, _d]),
+        "ns3d_solve_system": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, C.c_double, C.c_int32, _P(SolveInfo)]),
+        "ns3d_close": (C.c_int, [C.c_void_p]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    return lib
+
+
+_LIBS = {}
+
+
+def load(path):
+    """Load (once) a library implementing include/ns3d_capi.h."""
+    path = os.path.abspath(path)
+    if path not in _LIBS:
+        if not os.path.exists(path):
+            raise OSError("NS3D library not found: %s" % path)
+        _LIBS[path] = _declare(C.CDLL(path))
+    return _LIBS[path]
+
+
+def _ptr(a, ct):
+    return None if a is None else a.ctypes.data_as(_P(ct))
+
+
+def default_params(lib, **kw):
+    p = Params()
+    lib.ns3d_params_default(C.byref(p))
+    for k, v in kw.items():
+        if k == "method" and isinstance(v, str):
+            v = METHODS[v.upper()]
+        setattr(p, k, v)
+    return p
+
+
+class Solver:
+    """One solver instance (the C handle) on a given library."""
+
+    def __init__(self, lib, params, raw_xfastest, dims):
+        self.lib = lib
+        self.params = params
+        raw = np.ascontiguousarray(raw_xfastest, dtype=np.uint8).reshape(-1)
+        assert raw.size == dims[0] * dims[1] * dims[2]
+        h = C.c_void_p()
+        self._check(lib.ns3d_open(C.byref(params), _ptr(raw, C.c_uint8), int(dims[0]), int(dims[1]),
+                                  int(dims[2]), C.byref(h)))
+        self.h = h
+        s = Sizes()
+        self._check(lib.ns3d_get_sizes(h, C.byref(s)))
+        self.sizes = s
+
+    def _check(self, rc):
+        if rc < 0:
+            raise NS3DError(rc, self.lib.ns3d_last_error().decode())
+        return rc
+
+    @property
+    def shape(self):
+        return (self.sizes.nx, self.sizes.ny, self.sizes.nz)
+
+    def n(self, sys):
+        s = self.sizes
+        return (s.nu, s.nv, s.nw, s.np)[sys]
+
+    def index_arrays(self):
+        nx, ny, nz = self.shape
+        p = np.empty((nx, ny, nz), np.int32)
+        u = np.empty((nx + 1, ny, nz), np.int32)
+        v = np.empty((nx, ny, nz), np.int32)
+        w = np.empty((nx, ny, nz), np.int32)
+        self._check(self.lib.ns3d_get_index_arrays(self.h, _ptr(p, C.c_int32), _ptr(u, C.c_int32),
+                                                   _ptr(v, C.c_int32), _ptr(w, C.c_int32)))
+        return p, u, v, w
+
+    def set_initial_fields(self, p=None, u=None, v=None, w=None):
+        a = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (p, u, v, w)]
+        self._check(self.lib.ns3d_set_initial_fields(self.h, *[_ptr(x, C.c_double) for x in a]))
+
+    def fields(self):
+        s = self.sizes
+        out = [np.empty(n, np.float64) for n in (s.np, s.nu, s.nv, s.nw)]
+        self._check(self.lib.ns3d_get_fields(self.h, *[_ptr(x, C.c_double) for x in out]))
+        return out
+
+    def set_fields(self, p=None, u=None, v=None, w=None):
+        a = [None if x is None else np.ascontiguousarray(x, np.float64) for x in (p, u, v, w)]
+        self._check(self.lib.ns3d_set_fields(self.h, *[_ptr(x, C.c_double) for x in a]))
+
+    def field_images(self):
+        nx, ny, nz = self.shape
+        p = np.empty((nx, ny, nz)); u = np.empty((nx + 1, ny, nz))
+        v = np.empty((nx, ny, nz)); w = np.empty((nx, ny, nz)); va = np.empty((nx, ny, nz, 3))
+        self._check(self.lib.ns3d_get_field_images(self.h, *[_ptr(x, C.c_double) for x in (p, u, v, w, va)]))
+        return p, u, v, w, va
+
+    def set_output(self, directory, stem, write_fields=True):
+        d = None if directory is None else str(directory).encode()
+        self._check(self.lib.ns3d_set_output(self.h, d, stem.encode(), int(bool(write_fields))))
+
+    def solve(self):
+        self._check(self.lib.ns3d_solve(self.h))
+        return self.result()
+
+    def result(self):
+        r = Result()
+        self._check(self.lib.ns3d_get_result(self.h, C.byref(r)))
+        return r
+
+    def assemble_momentum(self):
+        self._check(self.lib.ns3d_assemble_momentum(self.h))
+
+    def assemble_pressure_correction(self, simplec=True):
+        self._check(self.lib.ns3d_assemble_pressure_correction(self.h, int(bool(simplec))))
+
+    def assemble_pressure(self, relax=True):
+        self._check(self.lib.ns3d_assemble_pressure(self.h, int(bool(relax))))
+
+    def system(self, sys):
+        n = self.n(sys)
+        coef = np.empty((7, n)); nbr = np.empty((6, n), np.int32)
+        rhs = np.empty(n); rs = np.empty(n)
+        self._check(self.lib.ns3d_get_system(self.h, sys, _ptr(coef, C.c_double), _ptr(nbr, C.c_int32),
+                                             _ptr(rhs, C.c_double), _ptr(rs, C.c_double)))
+        return coef, nbr, rhs, rs
+
+    def solve_system(self, sys, x, tol, maxit, rhs=None):
+        x = np.ascontiguousarray(x, np.float64).copy()
+        info = SolveInfo()
+        b = None if rhs is None else np.ascontiguousarray(rhs, np.float64)
+        self._check(self.lib.ns3d_solve_system(self.h, sys, _ptr(b, C.c_double), _ptr(x, C.c_double),
+                                               float(tol), int(maxit), C.byref(info)))
+        return x, info
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.ns3d_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,119 @@
+// device.cuh -- device-side data layout of the NS3D GB300 solver.
+//
+// HBM layout (all int32 / FP64, one allocation family per solver instance):
+//   image      uint8  nx*ny*nz        binarized, rotated, padded (0 = fluid)
+//   pmap, vmap, wmap  int32 nx*ny*nz  index maps (-1 = no node), C order
+//   umap       int32 (nx+1)*ny*nz
+//   per system (u, v, w on faces; p on cells), rows padded to a multiple of
+//   the 1024-row reduction chunk:
+//     cell     int32 [npad]     row -> linear position in its map
+//     coef     f64   [7][npad]  slots P,W,E,S,N,B,T (structure of arrays)
+//     nbr      int32 [6][npad]  columns of W,E,S,N,B,T (-1 = no entry)
+//     rhs, rowsum, invdiag  f64 [npad]
+//   Krylov workspace per system: r, r0, p, v, y, s, z, t  f64 [npad]
+#pragma once
+
+#include "common.cuh"
+
+namespace ns3d {
+
+enum Slot { SP = 0, SW = 1, SE = 2, SS = 3, SN = 4, SB = 5, ST = 6 };
+
+struct Grid {
+    int nx, ny, nz;
+    const int *pmap, *umap, *vmap, *wmap;
+    __host__ __device__ __forceinline__ long lin(int i, int j, int k) const { return ((long)i * ny + j) * nz + k; }
+    __device__ __forceinline__ int P(int i, int j, int k) const { return pmap[lin(i, j, k)]; }
+    __device__ __forceinline__ int U(int i, int j, int k) const { return umap[lin(i, j, k)]; }
+    __device__ __forceinline__ int V(int i, int j, int k) const { return vmap[lin(i, j, k)]; }
+    __device__ __forceinline__ int W(int i, int j, int k) const { return wmap[lin(i, j, k)]; }
+    __device__ __forceinline__ void ijk(long c, int &i, int &j, int &k) const {
+        k = (int)(c % nz);
+        long t = c / nz;
+        j = (int)(t % ny);
+        i = (int)(t / ny);
+    }
+    // SafeVectorValue (src/NSBase.cxx:1757-1771): the node value or 0
+    __device__ __forceinline__ double su(const double *f, int i, int j, int k) const {
+        if (i >= nx + 1 || i < 0 || j >= ny || j < 0 || k >= nz || k < 0) return 0;
+        int r = U(i, j, k);
+        return r > -1 ? f[r] : 0;
+    }
+    __device__ __forceinline__ double sv(const double *f, int i, int j, int k) const {
+        if (i >= nx || i < 0 || j >= ny || j < 0 || k >= nz || k < 0) return 0;
+        int r = V(i, j, k);
+        return r > -1 ? f[r] : 0;
+    }
+    __device__ __forceinline__ double sw(const double *f, int i, int j, int k) const {
+        if (i >= nx || i < 0 || j >= ny || j < 0 || k >= nz || k < 0) return 0;
+        int r = W(i, j, k);
+        return r > -1 ? f[r] : 0;
+    }
+};
+
+struct SysView {
+    int n, npad, nchunks;
+    const int *cell;
+    double *coef;  // [7][npad]
+    int *nbr;      // [6][npad]
+    double *rhs, *rowsum, *invdiag;
+    __device__ __forceinline__ double &c(int s, int r) const { return coef[(size_t)s * npad + r]; }
+    __device__ __forceinline__ int nb(int s, int r) const { return nbr[(size_t)s * npad + r]; }
+};
+
+// Row sum / product in ascending column order.  For every system of this
+// solver the ascending order of a row's columns is W,S,B,P,T,N,E except that
+// W comes after S and B when W is the previous row, and E comes before T and
+// N when E is the next row (the u outlet faces are numbered right after the
+// last cell's west face).
+template <class Op>
+__device__ __forceinline__ double row_ordered(int row, int nW, int nE, int nS, int nN, int nB, int nT, Op op) {
+    double acc = 0.0;
+    if (nW == row - 1) {
+        if (nS >= 0) acc = op(acc, SS, nS);
+        if (nB >= 0) acc = op(acc, SB, nB);
+        acc = op(acc, SW, nW);
+    } else {
+        if (nW >= 0) acc = op(acc, SW, nW);
+        if (nS >= 0) acc = op(acc, SS, nS);
+        if (nB >= 0) acc = op(acc, SB, nB);
+    }
+    acc = op(acc, SP, row);
+    if (nE == row + 1) {
+        acc = op(acc, SE, nE);
+        if (nT >= 0) acc = op(acc, ST, nT);
+        if (nN >= 0) acc = op(acc, SN, nN);
+    } else {
+        if (nT >= 0) acc = op(acc, ST, nT);
+        if (nN >= 0) acc = op(acc, SN, nN);
+        if (nE >= 0) acc = op(acc, SE, nE);
+    }
+    return acc;
+}
+
+// ---- BiCGSTAB state of one system ---------------------------------------
+struct KState {
+    double rho, alpha, w, beta;   // Krylov scalars (beta = next step's beta)
+    double r0_sqnorm, rhs_sqnorm, tol, tol2, rr, error;
+    int iter, maxit, restarts;
+    int done;      // loop finished
+    int paused;    // restart requested: host recomputes the residual
+    int info;      // Eigen ComputationInfo
+    int zero_rhs;  // rhs == 0: x = 0, iterations() = maxit
+    int work;      // iterations executed, restarts included (work accounting)
+    unsigned int counter;  // arrivals of chunks in the current kernel
+    unsigned int pad2_;
+};
+
+struct KSys {  // one system of a solve set (device array)
+    int n, npad, nchunks, chunk_begin;
+    const double *coef;
+    const int *nbr;
+    const double *invdiag;
+    const double *b;
+    double *x, *r, *r0, *p, *v, *y, *s, *z, *t;
+    double *part;  // [nchunks][2]
+    KState *st;
+};
+
+}  // namespace ns3d

@@ -1,0 +1,141 @@
+// runtime.h -- device memory ownership and the batched Krylov driver.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "device.cuh"
+#include "kernels.h"
+
+namespace ns3d {
+
+struct CudaError : std::runtime_error {
+    cudaError_t code;
+    CudaError(cudaError_t e, const char *expr, const char *file, int line)
+        : std::runtime_error(std::string(cudaGetErrorString(e)) + " in " + expr + " (" + file + ":" +
+                             std::to_string(line) + ")"),
+          code(e) {}
+};
+
+struct ApiError : std::runtime_error {
+    int code;
+    ApiError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+// owning device buffer
+template <class T>
+struct DBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    DBuf() = default;
+    DBuf(const DBuf &) = delete;
+    DBuf &operator=(const DBuf &) = delete;
+    ~DBuf() { release(); }
+    void alloc(size_t count) {
+        release();
+        n = count;
+        if (count == 0) return;
+        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        if (e != cudaSuccess) {
+            p = nullptr;
+            n = 0;
+            cudaGetLastError();
+            throw ApiError(NS3D_ERR_OOM, "device allocation of " + std::to_string(count * sizeof(T)) + " bytes failed");
+        }
+    }
+    void alloc_zero(size_t count, cudaStream_t st) {
+        alloc(count);
+        if (count) NS3D_CUDA_CHECK(cudaMemsetAsync(p, 0, count * sizeof(T), st));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+// pinned host buffer
+template <class T>
+struct HBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    HBuf() = default;
+    HBuf(const HBuf &) = delete;
+    HBuf &operator=(const HBuf &) = delete;
+    ~HBuf() {
+        if (p) cudaFreeHost(p);
+    }
+    void alloc(size_t count) {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        n = count;
+        if (count) NS3D_CUDA_CHECK(cudaMallocHost((void **)&p, count * sizeof(T)));
+    }
+};
+
+inline int pad_rows(int n) { return ((n + CH - 1) / CH) * CH; }
+
+// one linear system (momentum component or pressure) and its Krylov workspace
+struct DevSys {
+    int n = 0, npad = 0, nchunks = 0, d0 = 0;
+    DBuf<int> cell;
+    DBuf<double> coef;
+    DBuf<int> nbr;
+    DBuf<double> rhs, rowsum, invdiag;
+    DBuf<double> r, r0, p, v, y, s, z, t, part;
+    void allocate(int rows, int first_extent, cudaStream_t st);
+    SysView view() const {
+        SysView sv;
+        sv.n = n;
+        sv.npad = npad;
+        sv.nchunks = nchunks;
+        sv.cell = cell.p;
+        sv.coef = coef.p;
+        sv.nbr = nbr.p;
+        sv.rhs = rhs.p;
+        sv.rowsum = rowsum.p;
+        sv.invdiag = invdiag.p;
+        return sv;
+    }
+    size_t device_bytes() const;
+};
+
+struct SolveItem {
+    DevSys *sys;
+    double *x;        // guess in, solution out (npad doubles)
+    const double *b;  // right-hand side (npad doubles)
+    double tol;
+    int maxit;
+};
+
+struct SolveOutcome {
+    int iters = 0, info = 0, work = 0;
+    double error = 0;
+    bool valid = false;
+};
+
+// A set of systems solved together by the batched BiCGSTAB kernels.
+class KrylovSet {
+  public:
+    void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out);
+    const KState *device_state(int i) const { return st_.p + i; }
+    long launches() const { return launches_; }
+    void reset_launch_count() { launches_ = 0; }
+
+  private:
+    void configure(const std::vector<SolveItem> &items, cudaStream_t st);
+    DBuf<KSys> ksys_;
+    DBuf<int> chunk_sys_;
+    DBuf<KState> st_;
+    HBuf<KState> h_st_, h_up_;
+    HBuf<KSys> h_ksys_;
+    std::vector<KSys> cur_;
+    int nsys_ = 0, total_chunks_ = 0;
+    int prev_iters_ = 8;
+    long launches_ = 0;
+};
+
+}  // namespace ns3d

@@ -1,0 +1,1071 @@
+// solver.cu -- host orchestration of the NS3D solve on one GB300 and the
+// C-ABI of include/ns3d_capi.h.
+//
+// Everything inside the outer loop runs on the device (kernels in
+// geometry.cu, physics.cu, krylov.cu); the host keeps the control flow of the
+// reference drivers (SIMPLECSOLVER::Solve src/SIMPLEC.cxx:73-232,
+// SIMPLERSOLVER::Solve src/SIMPLER.cxx:75-270, SIMPLERRSOLVER::Solve
+// src/SIMPLERR.cxx:75-280, IDEALSOLVER::Solve src/IDEAL.cxx:75-281), the
+// scalar relaxation state machine (RelaxControl, src/NSBase.cxx:196-301) and
+// the INFO/RES logs.  Per outer iteration only a few scalars come back to the
+// host: solver statuses, K, the divergence norms and the pressure-correction
+// statistics.
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <ctime>
+#include <list>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "hostio.h"
+#include "runtime.h"
+
+namespace ns3d {
+
+// ============================ runtime =======================================
+void DevSys::allocate(int rows, int first_extent, cudaStream_t st) {
+    n = rows;
+    npad = pad_rows(std::max(rows, 1));
+    nchunks = (rows + CH - 1) / CH;
+    d0 = first_extent;
+    cell.alloc_zero(npad, st);
+    coef.alloc_zero((size_t)7 * npad, st);
+    nbr.alloc(6 * (size_t)npad);
+    NS3D_CUDA_CHECK(cudaMemsetAsync(nbr.p, 0xff, nbr.n * sizeof(int), st));
+    rhs.alloc_zero(npad, st);
+    rowsum.alloc_zero(npad, st);
+    invdiag.alloc_zero(npad, st);
+    DBuf<double> *ws[] = {&r, &r0, &p, &v, &y, &s, &z, &t};
+    for (auto *b : ws) b->alloc_zero(npad, st);
+    part.alloc_zero((size_t)2 * std::max(nchunks, 1), st);
+}
+
+size_t DevSys::device_bytes() const {
+    return cell.n * 4 + coef.n * 8 + nbr.n * 4 + (rhs.n + rowsum.n + invdiag.n) * 8 + 8 * (size_t)npad * 8 +
+           part.n * 8;
+}
+
+void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
+    std::vector<KSys> ks;
+    int chunk = 0;
+    for (const SolveItem &it : items) {
+        KSys k;
+        DevSys &S = *it.sys;
+        k.n = S.n;
+        k.npad = S.npad;
+        k.nchunks = S.nchunks;
+        k.chunk_begin = chunk;
+        chunk += S.nchunks;
+        k.coef = S.coef.p;
+        k.nbr = S.nbr.p;
+        k.invdiag = S.invdiag.p;
+        k.b = it.b;
+        k.x = it.x;
+        k.r = S.r.p; k.r0 = S.r0.p; k.p = S.p.p; k.v = S.v.p; k.y = S.y.p;
+        k.s = S.s.p; k.z = S.z.p; k.t = S.t.p;
+        k.part = S.part.p;
+        k.st = nullptr;
+        ks.push_back(k);
+    }
+    const int ns = (int)ks.size();
+    bool same = ns == nsys_ && chunk == total_chunks_ && cur_.size() == ks.size();
+    if (same)
+        for (int i = 0; i < ns; ++i)
+            if (std::memcmp(&cur_[i], &ks[i], sizeof(KSys) - sizeof(KState *)) != 0) same = false;
+    if (same) return;
+    if ((int)st_.n < ns) {
+        st_.alloc_zero(ns, st);
+        h_st_.alloc(ns);
+        h_up_.alloc(ns);
+        h_ksys_.alloc(ns);
+    }
+    for (int i = 0; i < ns; ++i) ks[i].st = st_.p + i;
+    if ((int)ksys_.n < ns) ksys_.alloc(ns);
+    std::memcpy(h_ksys_.p, ks.data(), ns * sizeof(KSys));
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(ksys_.p, h_ksys_.p, ns * sizeof(KSys), cudaMemcpyHostToDevice, st));
+    std::vector<int> cs((size_t)std::max(chunk, 1));
+    for (int i = 0; i < ns; ++i)
+        for (int c = 0; c < ks[i].nchunks; ++c) cs[(size_t)ks[i].chunk_begin + c] = i;
+    chunk_sys_.alloc(cs.size());
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(chunk_sys_.p, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
+    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));  // cs is a host temporary
+    cur_ = ks;
+    nsys_ = ns;
+    total_chunks_ = chunk;
+}
+
+void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out) {
+    configure(items, st);
+    const int ns = nsys_;
+    out.assign(ns, SolveOutcome());
+    int maxit = 0;
+    for (int i = 0; i < ns; ++i) {
+        KState z;
+        std::memset(&z, 0, sizeof z);
+        z.tol = items[i].tol;
+        z.maxit = items[i].maxit;
+        if (items[i].sys->n == 0) {  // no rows: nothing to launch, report like a zero right-hand side
+            z.done = 1;
+            z.zero_rhs = 1;
+            z.iter = z.maxit;
+            z.error = z.tol;
+        }
+        h_up_.p[i] = z;
+        maxit = std::max(maxit, items[i].maxit);
+    }
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(st_.p, h_up_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
+    launch_krylov_init(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+    launches_ += 2;
+    // Iterations are issued in batches; finished systems make the kernels
+    // return at once, so a batch may overshoot the last iteration harmlessly.
+    // Restarts reset the iteration counter once, so 2*maxit bounds the loop.
+    const long cap = 2L * maxit + 64;
+    long issued = 0;
+    int batch = std::max(1, std::min(32, prev_iters_ / 2));
+    int max_iters = 0;
+    while (true) {
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
+        NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+        bool all_done = true, any_paused = false;
+        for (int i = 0; i < ns; ++i) {
+            if (!h_st_.p[i].done) all_done = false;
+            if (h_st_.p[i].paused && !h_st_.p[i].done) any_paused = true;
+        }
+        if (all_done) break;
+        if (issued >= cap) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
+        if (any_paused) {
+            launch_krylov_restart(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+            launches_ += 1;
+        }
+        for (int b = 0; b < batch; ++b) launch_krylov_iteration(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+        launches_ += 5L * batch;
+        issued += batch;
+        batch = std::min(64, batch * 2);
+    }
+    for (int i = 0; i < ns; ++i) {
+        const KState &k = h_st_.p[i];
+        out[i].iters = k.iter;
+        out[i].info = k.info;
+        out[i].error = k.error;
+        out[i].work = k.work;
+        out[i].valid = true;
+        if (!k.zero_rhs) max_iters = std::max(max_iters, k.work);
+    }
+    prev_iters_ = std::max(2, max_iters);
+}
+
+// ============================ solver instance ================================
+static thread_local std::string g_err;
+
+static int set_error(int code, const std::string &m) {
+    g_err = m;
+    return code;
+}
+
+struct Scalars {
+    double Q = 0, v_moy = 0, K = 0, normdiv = 0, reldiv = 0, velocityNorm = 0, maxdiv = 0, MaxDeltaV = 0;
+};
+
+}  // namespace ns3d
+
+using namespace ns3d;
+
+struct ns3d_handle {
+    ns3d_params prm;
+    int rnx = 0, rny = 0, rnz = 0;  // raw image
+    int nx = 0, ny = 0, nz = 0;     // solver frame
+    int np = 0, nu = 0, nv = 0, nw = 0;
+    cudaStream_t stream = nullptr;
+
+    DBuf<uint8_t> img;
+    DBuf<int> pmap, umap, vmap, wmap;
+    DevSys U, V, W, P;
+    // fields and work vectors (npad of their system)
+    DBuf<double> p, u, v, w, pc, ptemp, utemp, vtemp, wtemp, uh, vh, wh, ut, vt, wt;
+    DBuf<double> diag_part;
+    DBuf<DiagOut> diag;
+    HBuf<DiagOut> h_diag;
+    KrylovSet kmom, kp;
+
+    // physical constants and relaxation state (NavierStokesBase members)
+    double dx, dy, dz, mu, rho, p0, p1, gradp, alpha0, beta0, alpha, beta;
+    double p_inlet = 0, p_outlet = 0, schemefactor, min_alpha, min_beta, relax, speedup, maxconvdelta;
+    double RMR = 0, old_RMR = 0, deltaRMR, pcmax = 0, pcmin = 0, pcnorm = 0;
+    int border;
+    std::list<double> avgRMR;
+    SolveOutcome su, sv, sw, sp;
+
+    ns3d_result res;
+    std::string outdir, stem;
+    bool write_fields = false, have_out = false;
+    TextLog info, resl;
+
+    Grid grid() const {
+        Grid g;
+        g.nx = nx; g.ny = ny; g.nz = nz;
+        g.pmap = pmap.p; g.umap = umap.p; g.vmap = vmap.p; g.wmap = wmap.p;
+        return g;
+    }
+    Phys phys() const {
+        Phys ph;
+        ph.dx = dx; ph.dy = dy; ph.dz = dz; ph.mu = mu; ph.rho = rho; ph.alpha = alpha; ph.beta = beta;
+        ph.p0 = p0; ph.p1 = p1; ph.schemefactor = schemefactor;
+        return ph;
+    }
+    ~ns3d_handle() {
+        if (stream) {
+            cudaStreamSynchronize(stream);
+            cudaStreamDestroy(stream);
+        }
+    }
+
+    // ---------------------------------------------------------------------
+    void build(const uint8_t *raw, int rx, int ry, int rz);
+    void default_fields();
+    void assemble_all_momentum();
+    void momentum_rhs();
+    void compute_velocity_field(bool limit, double dvmax);
+    void log_solve(const char *comp, const SolveOutcome &o);
+    void log_pressure_status(const SolveOutcome &o);
+    void compute_pressure_correction();
+    void compute_pressure_field();
+    void correct_pressure_field();
+    void permeability(Scalars &s);
+    void divergence(Scalars &s);
+    void diagnostics(Scalars &s);
+    void relax_control(bool beta_cst);
+    bool check_convergence(double res_, double tol) const;
+    void pressure_step(bool relax_p, const double *uc, const double *vc, const double *wc, const double *uold,
+                       const double *vold, const double *wold, double *ux, double *vx, double *wx);
+    void hats(const double *uc, const double *vc, const double *wc, const double *uold, const double *vold,
+              const double *wold);
+    void res_row(int it, const Scalars &s);
+    void fields_to_image(const std::string &file);
+    void save_snapshot(int it, int &savecounter);
+    void header(const char *name, const char *maxname);
+    void finish(const char *name, int it, const Scalars &s, std::chrono::steady_clock::time_point t0, time_t start);
+    void initial_velocity(Scalars &s);
+    void run_simplec();
+    void run_simpler_family(int method);
+    void old_rmr_update(int it) {
+        if (it > 1) {
+            if (RMR < old_RMR) old_RMR = RMR;
+        } else {
+            old_RMR = RMR;
+        }
+    }
+    void sync() { NS3D_CUDA_CHECK(cudaStreamSynchronize(stream)); }
+    void d2d(double *dst, const double *src, size_t n) {
+        if (n) NS3D_CUDA_CHECK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
+    }
+};
+
+// ---- geometry -----------------------------------------------------------------
+void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
+    rnx = rx; rny = ry; rnz = rz;
+    int ax = rx, ay = ry, az = rz;
+    if (prm.direction == 2) std::swap(ax, ay);
+    else if (prm.direction == 3) std::swap(ax, az);
+    nx = ax + 2 * std::max(prm.border, 0);
+    ny = ay;
+    nz = az;
+    const long N = (long)nx * ny * nz, NU = (long)(nx + 1) * ny * nz;
+    if (NU > 0x7fffffffL) throw ApiError(NS3D_ERR_ARG, "image too large for int32 indices");
+    DBuf<uint8_t> draw;
+    draw.alloc((size_t)rx * ry * rz);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(draw.p, raw, draw.n, cudaMemcpyHostToDevice, stream));
+    img.alloc(N);
+    launch_build_image(draw.p, rx, ry, rz, prm.direction, std::max(prm.border, 0), prm.porevalue, img.p, nx, ny, nz,
+                       stream);
+    pmap.alloc(N); vmap.alloc(N); wmap.alloc(N); umap.alloc(NU);
+    for (DBuf<int> *m : {&pmap, &vmap, &wmap, &umap}) NS3D_CUDA_CHECK(cudaMemsetAsync(m->p, 0xff, m->n * 4, stream));
+    // cell tables sized by the worst case, shrunk after the counts are known
+    DBuf<int> pcell, ucell, vcell, wcell;
+    pcell.alloc(N); ucell.alloc(NU); vcell.alloc(N); wcell.alloc(N);
+    DBuf<int4> blk, tot;
+    blk.alloc(index_build_blocks(N));
+    tot.alloc(1);
+    launch_index_build(img.p, nx, ny, nz, blk.p, tot.p, pmap.p, umap.p, vmap.p, wmap.p, pcell.p, ucell.p, vcell.p,
+                       wcell.p, stream);
+    int4 t;
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(&t, tot.p, sizeof(int4), cudaMemcpyDeviceToHost, stream));
+    NS3D_CUDA_CHECK(cudaStreamSynchronize(stream));
+    np = t.x; nu = t.y; nv = t.z; nw = t.w;
+    U.allocate(nu, nx + 1, stream);
+    V.allocate(nv, nx, stream);
+    W.allocate(nw, nx, stream);
+    P.allocate(np, nx, stream);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(U.cell.p, ucell.p, (size_t)nu * 4, cudaMemcpyDeviceToDevice, stream));
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(V.cell.p, vcell.p, (size_t)nv * 4, cudaMemcpyDeviceToDevice, stream));
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(W.cell.p, wcell.p, (size_t)nw * 4, cudaMemcpyDeviceToDevice, stream));
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(P.cell.p, pcell.p, (size_t)np * 4, cudaMemcpyDeviceToDevice, stream));
+    launch_nbr_mom(umap.p, nx + 1, ny, nz, U.cell.p, nu, U.npad, U.nbr.p, nz > 1, stream);
+    launch_nbr_mom(vmap.p, nx, ny, nz, V.cell.p, nv, V.npad, V.nbr.p, nz > 1, stream);
+    launch_nbr_mom(wmap.p, nx, ny, nz, W.cell.p, nw, W.npad, W.nbr.p, 1, stream);
+    launch_nbr_p(grid(), P.cell.p, np, P.npad, P.nbr.p, stream);
+    for (DBuf<double> *f : {&p, &pc, &ptemp}) f->alloc_zero(P.npad, stream);
+    for (DBuf<double> *f : {&u, &utemp, &uh, &ut}) f->alloc_zero(U.npad, stream);
+    for (DBuf<double> *f : {&v, &vtemp, &vh, &vt}) f->alloc_zero(V.npad, stream);
+    for (DBuf<double> *f : {&w, &wtemp, &wh, &wt}) f->alloc_zero(W.npad, stream);
+    int maxch = std::max({P.nchunks, (int)(((long)ny * nz + CH - 1) / CH), 1});
+    diag_part.alloc_zero((size_t)5 * maxch, stream);
+    diag.alloc_zero(1, stream);
+    h_diag.alloc(1);
+    NS3D_CUDA_CHECK(cudaStreamSynchronize(stream));  // temporaries are freed on return
+}
+
+void ns3d_handle::default_fields() {
+    for (DBuf<double> *f : {&p, &pc, &u, &v, &w})
+        if (f->n) NS3D_CUDA_CHECK(cudaMemsetAsync(f->p, 0, f->n * 8, stream));
+    launch_default_pressure(grid(), P.view(), p0, p1, p.p, stream);
+}
+
+// ---- momentum -------------------------------------------------------------------
+// AssembleAllMomentum, src/NSBase.cxx:853-884 (the Jacobi factorization is
+// the inverse diagonal, computed in the assembly epilogue with the row sums)
+void ns3d_handle::assemble_all_momentum() {
+    const Grid g = grid();
+    const Phys ph = phys();
+    launch_assemble_momentum(0, g, ph, U.view(), u.p, v.p, w.p, stream);
+    launch_assemble_momentum(1, g, ph, V.view(), u.p, v.p, w.p, stream);
+    if (nw > 0) launch_assemble_momentum(2, g, ph, W.view(), u.p, v.p, w.p, stream);
+}
+
+void ns3d_handle::momentum_rhs() {
+    const Grid g = grid();
+    const Phys ph = phys();
+    launch_momentum_rhs(0, g, ph, U.view(), p.p, u.p, stream);
+    launch_momentum_rhs(1, g, ph, V.view(), p.p, v.p, stream);
+    if (nw > 0) launch_momentum_rhs(2, g, ph, W.view(), p.p, w.p, stream);
+}
+
+void ns3d_handle::log_solve(const char *comp, const SolveOutcome &o) {
+    info.s("Solving for component ").s(comp).s(" in ").i(o.iters).s(" iterations (status ").i(o.info).s(")").nl();
+}
+
+// ComputeVelocityField, src/NSBase.cxx:1773-1884: the three components are
+// solved together by one batched BiCGSTAB launch sequence
+void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
+    momentum_rhs();
+    d2d(utemp.p, u.p, U.npad);
+    d2d(vtemp.p, v.p, V.npad);
+    if (nw > 0) d2d(wtemp.p, w.p, W.npad);
+    std::vector<SolveItem> items = {{&U, u.p, U.rhs.p, prm.vsolvertol, prm.maxitsolver},
+                                    {&V, v.p, V.rhs.p, prm.vsolvertol, prm.maxitsolver}};
+    if (nw > 0) items.push_back({&W, w.p, W.rhs.p, prm.vsolvertol, prm.maxitsolver});
+    std::vector<SolveOutcome> out;
+    kmom.run(items, stream, out);
+    launch_velocity_post(utemp.p, u.p, nu, kmom.device_state(0), limit, dvmax, stream);
+    launch_velocity_post(vtemp.p, v.p, nv, kmom.device_state(1), limit, dvmax, stream);
+    if (nw > 0) launch_velocity_post(wtemp.p, w.p, nw, kmom.device_state(2), limit, dvmax, stream);
+    su = out[0];
+    sv = out[1];
+    if (nw > 0) sw = out[2];
+    for (const SolveOutcome &o : out) {
+        res.krylov_iterations += o.work;
+    }
+    res.krylov_rows += (int64_t)su.work * nu + (int64_t)sv.work * nv + (nw > 0 ? (int64_t)sw.work * nw : 0);
+    log_solve("u", su);
+    log_solve("v", sv);
+    if (nw > 0) log_solve("w", sw);
+}
+
+// ---- pressure ---------------------------------------------------------------------
+void ns3d_handle::log_pressure_status(const SolveOutcome &o) {
+    if (o.info == NS3D_SUCCESS) {
+        info.i(o.iters).s(" iterations (status ").i(o.info).s(")").nl();
+    } else {
+        if (o.info == NS3D_NUMERICAL_ISSUE) info.s("Numerical Issue (iterations:").i(o.iters).s("). ");
+        else if (o.info == NS3D_NO_CONVERGENCE) info.s("No convergence (iterations:").i(o.iters).s("). ");
+        else if (o.info == NS3D_INVALID_INPUT) info.s("Invalid input (iterations:").i(o.iters).s("). ");
+        info.s("Residual: ").d(o.error).nl();
+    }
+}
+
+// ComputePressureCorrection, src/NSBase.cxx:2337-2365
+void ns3d_handle::compute_pressure_correction() {
+    info.s("Solving for pressure correction : ");
+    std::vector<SolveOutcome> out;
+    kp.run({{&P, pc.p, P.rhs.p, prm.pcsolvertol, prm.maxitsolver}}, stream, out);
+    sp = out[0];
+    res.krylov_iterations += sp.work;
+    res.krylov_rows += (int64_t)sp.work * np;
+    log_pressure_status(sp);
+}
+
+// ComputePressureField, src/NSBase.cxx:2383-2423
+void ns3d_handle::compute_pressure_field() {
+    double tol = prm.psolvertol;
+    info.s("Solving for pressure in : ");
+    d2d(ptemp.p, p.p, P.npad);
+    std::vector<SolveOutcome> out;
+    kp.run({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, stream, out);
+    sp = out[0];
+    res.krylov_iterations += sp.work;
+    res.krylov_rows += (int64_t)sp.work * np;
+    while (sp.iters == 0 && sp.info == NS3D_SUCCESS && tol > 1e-15) {
+        tol *= 0.1;
+        kp.run({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, stream, out);
+        sp = out[0];
+        res.krylov_iterations += sp.work;
+        res.krylov_rows += (int64_t)sp.work * np;
+    }
+    if (sp.iters > 0) d2d(p.p, ptemp.p, P.npad);
+    log_pressure_status(sp);
+}
+
+// CorrectPressureField, src/NSBase.cxx:2367-2380
+void ns3d_handle::correct_pressure_field() {
+    launch_correct_pressure(P.view(), pc.p, p.p, beta, diag_part.p, diag.p, stream);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
+    sync();
+    const DiagOut &d = *h_diag.p;
+    pcmax = beta * d.pcmax;
+    pcmin = beta * d.pcmin;
+    pcnorm = beta * std::sqrt(d.pcsq);
+    info.s("Correction de pression maximale et minimale: ").d(pcmax).s(", ").d(pcmin).nl();
+    info.s("Norme de la correction de pression : ").d(pcnorm).nl();
+}
+
+// ---- diagnostics ------------------------------------------------------------------
+// ComputePermeability, src/NSBase.cxx:1886-1956
+void ns3d_handle::permeability(Scalars &s) {
+    launch_permeability(grid(), u.p, p.p, border, diag_part.p, diag.p, stream);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
+    sync();
+    const DiagOut &d = *h_diag.p;
+    const double sx = dy * dz;
+    double v_moy = d.v_sum;
+    if (border <= 0) {
+        p_inlet = p0;
+        p_outlet = p1;
+    } else {
+        p_inlet = d.p_in_sum;
+        p_outlet = d.p_out_sum;
+        int ci = (int)d.cnt_in, co = (int)d.cnt_out;
+        if (ci > 0) p_inlet /= ci;
+        if (co > 0) p_outlet /= co;
+    }
+    s.Q = v_moy * sx;
+    v_moy /= (ny * nz);
+    s.v_moy = v_moy;
+    if (std::fabs(p_inlet - p_outlet) > 0.0)
+        s.K = v_moy * mu * dx * (nx - 2 * border) / (p_inlet - p_outlet);
+    else
+        s.K = 0.0;
+}
+
+// ComputeDiv, src/NSBase.cxx:1958-2080
+void ns3d_handle::divergence(Scalars &s) {
+    launch_divergence(grid(), phys(), P.view(), u.p, v.p, w.p, diag_part.p, diag.p, stream);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
+    sync();
+    const DiagOut &d = *h_diag.p;
+    s.normdiv = std::sqrt(d.sumdiv2);
+    s.velocityNorm = d.sumvel / np;
+    s.maxdiv = d.maxdiv;
+    s.MaxDeltaV = d.maxdv;
+}
+
+void ns3d_handle::diagnostics(Scalars &s) {
+    permeability(s);
+    divergence(s);
+    RMR = s.MaxDeltaV / std::fabs(s.v_moy);
+    s.reldiv = (nx * dx + ny * dy + nz * dz) * s.maxdiv / (3 * s.v_moy);
+    info.s("Permeability K (m²): ").d(s.K).nl();
+}
+
+// RelaxControl, src/NSBase.cxx:196-301
+void ns3d_handle::relax_control(bool beta_cst) {
+    const size_t size = 30;
+    bool isDecreasing = false;
+    if (RMR > old_RMR * maxconvdelta) {
+        alpha = std::max(min_alpha, alpha - relax);
+        if (!beta_cst) beta = std::max(min_beta, beta - relax);
+        old_RMR *= 1.1;
+        info.s("Relative Mass Residual increases too much -> new relaxation parameter alpha, beta: ").d(alpha).s(", ")
+            .d(beta).nl();
+        if (!avgRMR.empty()) avgRMR.pop_front();
+    }
+    if (!avgRMR.empty()) isDecreasing = avgRMR.back() > RMR;
+    avgRMR.push_back(RMR);
+    if (avgRMR.size() > size) {
+        avgRMR.pop_front();
+        int i = 0, n1 = 0, n2 = 0;
+        double avg1 = 0, avg2 = 0;
+        for (double x : avgRMR) {
+            i += 1;
+            if (i < avgRMR.size() * 0.5) { avg1 += x; n1 += 1; }
+            else if (i >= avgRMR.size() * 0.5) { avg2 += x; n2 += 1; }
+        }
+        avg1 /= n1;
+        avg2 /= n2;
+        double delta = (avg2 - avg1) / std::max(avg1, avg2);
+        if (delta <= 0 && std::fabs(delta) < deltaRMR && isDecreasing == false) {
+            for (int c = 0; c < 15 && !avgRMR.empty(); ++c) avgRMR.pop_front();
+            alpha = std::min(alpha0, alpha - relax * 0.25);
+            if (!beta_cst) beta = std::max(min_beta, beta - relax * 0.25);
+            info.s("Simulation is oscillating -> new relaxation parameter alpha, beta: ").d(alpha).s(", ").d(beta).nl();
+        } else if (delta > 0 && isDecreasing == false) {
+            for (int c = 0; c < 15 && !avgRMR.empty(); ++c) avgRMR.pop_front();
+            alpha = std::max(min_alpha, alpha - relax);
+            if (!beta_cst) beta = std::max(min_beta, beta - relax);
+            info.s("Simulation is diverging -> new relaxation parameter alpha, beta: ").d(alpha).s(", ").d(beta).nl();
+        }
+    }
+}
+
+// CheckConvergence, src/NSBase.cxx:304-328
+bool ns3d_handle::check_convergence(double r, double tol) const {
+    if (r < tol) return true;
+    return su.iters == 0 && sv.iters == 0 && (nw == 0 || sw.iters == 0) && sp.iters == 0;
+}
+
+// ---- SIMPLER-family building blocks -------------------------------------------------
+void ns3d_handle::hats(const double *uc, const double *vc, const double *wc, const double *uold, const double *vold,
+                       const double *wold) {
+    const Phys ph = phys();
+    launch_hat(U.view(), ph, uc, uold, uh.p, stream);
+    launch_hat(V.view(), ph, vc, vold, vh.p, stream);
+    if (nw > 0) launch_hat(W.view(), ph, wc, wold, wh.p, stream);
+}
+
+// Compute_*_hat; AssemblePressure; ComputePressureField;
+// CorrectVelocityFieldSIMPLER into (ux, vx, wx)
+void ns3d_handle::pressure_step(bool relax_p, const double *uc, const double *vc, const double *wc, const double *uold,
+                                const double *vold, const double *wold, double *ux, double *vx, double *wx) {
+    hats(uc, vc, wc, uold, vold, wold);
+    const Grid g = grid();
+    const Phys ph = phys();
+    launch_assemble_pressure(0, relax_p ? 1 : 0, g, ph, P.view(), U.view(), V.view(), W.view(), uh.p, vh.p, wh.p,
+                             p.p, stream);
+    compute_pressure_field();
+    launch_correct_velocity_simpler(0, g, ph, U.view(), p.p, uh.p, ux, p0, p1, stream);
+    launch_correct_velocity_simpler(1, g, ph, V.view(), p.p, vh.p, vx, p0, p1, stream);
+    if (nw > 0) launch_correct_velocity_simpler(2, g, ph, W.view(), p.p, wh.p, wx, p0, p1, stream);
+}
+
+// ---- logs and outputs ------------------------------------------------------------------
+static const char *kResHeader =
+    "iteration, Q (m³/s), <u_out> (m/s), Max Rel Mass Res., K (m²), gradP (Pa/m), ||Div_u||, "
+    "Lref*(max DIV)/<u_out>, <||u||>, max DIV, it_u,it_v,it_w,it_pc";
+
+void ns3d_handle::res_row(int it, const Scalars &s) {
+    if (!resl.f) return;
+    resl.i(it).s(",").d(s.Q).s(",").d(s.v_moy).s(",").d(RMR).s(",").d(s.K).s(",");
+    resl.d((p_inlet - p_outlet) / (dx * (nx - 2 * border)));
+    resl.s(",").d(s.normdiv).s(",").d(s.reldiv).s(",").d(s.velocityNorm).s(", ").d(s.maxdiv).s(", ");
+    resl.i(su.valid ? su.iters : 0).s(",").i(sv.valid ? sv.iters : 0).s(",").i(sw.valid ? sw.iters : 0).s(",");
+    resl.i(sp.valid ? sp.iters : 0).nl();
+}
+
+// FieldsToImage, src/NSBase.cxx:330-476
+void ns3d_handle::fields_to_image(const std::string &file) {
+    const char *pre[5] = {"Vx-", "Vy-", "Vz-", "V-", "P-"};
+    std::string d = outdir.empty() ? std::string() : outdir + "/";
+    if (have_out && write_fields) {
+        const long N = (long)nx * ny * nz, NU = (long)(nx + 1) * ny * nz;
+        DBuf<double> dimg;
+        dimg.alloc((size_t)std::max(3 * N, NU));
+        std::vector<double> himg((size_t)std::max(3 * N, NU));
+        std::string err, dir = std::to_string(prm.direction) + "-";
+        auto dump = [&](const int *map, long cells, const double *f, int ex, const std::string &name) {
+            launch_gather_image(map, cells, f, dimg.p, stream);
+            NS3D_CUDA_CHECK(cudaMemcpyAsync(himg.data(), dimg.p, cells * 8, cudaMemcpyDeviceToHost, stream));
+            sync();
+            if (!vti_write_f64(d + name, himg.data(), ex, ny, nz, 1, err)) throw ApiError(NS3D_ERR_IO, err);
+        };
+        dump(umap.p, NU, u.p, nx + 1, std::string("Vx-") + dir + file);
+        dump(vmap.p, N, v.p, nx, std::string("Vy-") + dir + file);
+        dump(wmap.p, N, w.p, nx, std::string("Vz-") + dir + file);
+        launch_face_average(grid(), u.p, v.p, w.p, dimg.p, stream);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(himg.data(), dimg.p, 3 * N * 8, cudaMemcpyDeviceToHost, stream));
+        sync();
+        if (!vti_write_f64(d + "V-" + dir + file, himg.data(), nx, ny, nz, 3, err)) throw ApiError(NS3D_ERR_IO, err);
+        dump(pmap.p, N, p.p, nx, std::string("P-") + dir + file);
+    }
+    for (auto pr : pre) info.s("Writing ").s(pr).i(prm.direction).s("-").s(file).nl();
+}
+
+void ns3d_handle::save_snapshot(int it, int &savecounter) {
+    if (it % prm.save_step == 0 && it > 0) {
+        savecounter += 1;
+        if (savecounter > 3) savecounter = 1;
+        fields_to_image(stem + "-SAVE-" + std::to_string(savecounter) + ".vti");
+    }
+}
+
+void ns3d_handle::header(const char *name, const char *maxname) {
+    info.s("Initializing ").s(name).s(" algorithm").nl();
+    info.s("p0, p1 (Pa)= ").d(p0).s(",").d(p1).nl();
+    info.s("Pressure gradient (Pa/m)= ").d((p0 - p1) / (dx * nx)).nl();
+    info.s("inlet/outlet area (m²)= ").d(dy * dz * ny * nz).nl();
+    info.s(maxname).i(prm.maxitSIMPLE).nl();
+    if (resl.f) resl.s(kResHeader).nl();
+}
+
+void ns3d_handle::finish(const char *name, int it, const Scalars &s, std::chrono::steady_clock::time_point t0,
+                         time_t start) {
+    sync();
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    info.s("Norm of the velocity field divergence: ").d(s.normdiv).nl();
+    info.s("Relative divergence of the velocity field: ").d(s.reldiv).nl();
+    fields_to_image(stem + ".vti");
+    time_t end = time(0);
+    info.s(name).s(" terminated in ").i(it).s(" iteration and ").d(difftime(end, start)).s(" seconds").nl();
+    ns3d_result &R = res;
+    R.K = s.K; R.Q = s.Q; R.v_moy = s.v_moy; R.RMR = RMR;
+    R.normdiv = s.normdiv; R.reldiv = s.reldiv; R.velocityNorm = s.velocityNorm; R.maxdiv = s.maxdiv;
+    R.MaxDeltaV = s.MaxDeltaV; R.p_inlet = p_inlet; R.p_outlet = p_outlet; R.p0 = p0; R.p1 = p1;
+    R.alpha = alpha; R.beta = beta; R.pcmax = pcmax; R.pcmin = pcmin; R.pcnorm = pcnorm;
+    R.iterations = it;
+    R.it_u = su.valid ? su.iters : 0;
+    R.it_v = sv.valid ? sv.iters : 0;
+    R.it_w = sw.valid ? sw.iters : 0;
+    R.it_p = sp.valid ? sp.iters : 0;
+    R.seconds = secs;
+}
+
+void ns3d_handle::initial_velocity(Scalars &s) {
+    assemble_all_momentum();
+    compute_velocity_field(false, 0);
+    permeability(s);
+    info.s("Initial Permeability K (m²): ").d(s.K).nl();
+}
+
+// SIMPLECSOLVER::Solve, src/SIMPLEC.cxx:73-232
+void ns3d_handle::run_simplec() {
+    auto t0 = std::chrono::steady_clock::now();
+    time_t start = time(0);
+    Scalars s;
+    int savecounter = 0, it;
+    header("SIMPLEC", "Max number of SIMPLE iterations: ");
+    alpha = alpha0;
+    initial_velocity(s);
+    for (it = 0; it < prm.maxitSIMPLE; ++it) {
+        info.s("Iteration ").i(it).s("  ------------").nl();
+        if (it > 0) {
+            assemble_all_momentum();
+            compute_velocity_field(true, s.v_moy * std::min(1., alpha * 1.5));
+        }
+        diagnostics(s);
+        old_rmr_update(it);
+        res_row(it, s);
+        if (it > 1 && check_convergence(RMR, prm.simpletol)) {
+            info.s("Permeability K (m²): ").d(s.K).nl();
+            res.converged = 1;
+            break;
+        }
+        const Grid g = grid();
+        const Phys ph = phys();
+        launch_assemble_pressure(1, 0, g, ph, P.view(), U.view(), V.view(), W.view(), u.p, v.p, w.p, p.p, stream);
+        compute_pressure_correction();
+        const double dvmax = s.v_moy * alpha;
+        launch_correct_velocity(0, 1, g, ph, U.view(), pc.p, u.p, dvmax, stream);
+        launch_correct_velocity(1, 1, g, ph, V.view(), pc.p, v.p, dvmax, stream);
+        if (nw > 0) launch_correct_velocity(2, 1, g, ph, W.view(), pc.p, w.p, dvmax, stream);
+        correct_pressure_field();
+        Scalars after = s;
+        divergence(after);
+        s.MaxDeltaV = after.MaxDeltaV; s.normdiv = after.normdiv; s.velocityNorm = after.velocityNorm;
+        s.maxdiv = after.maxdiv;
+        save_snapshot(it, savecounter);
+        relax_control(true);
+    }
+    finish("SIMPLEC", it, s, t0, start);
+}
+
+// SIMPLERSOLVER::Solve src/SIMPLER.cxx:75-270, SIMPLERRSOLVER::Solve
+// src/SIMPLERR.cxx:75-280, IDEALSOLVER::Solve src/IDEAL.cxx:75-281
+void ns3d_handle::run_simpler_family(int method) {
+    auto t0 = std::chrono::steady_clock::now();
+    time_t start = time(0);
+    Scalars s;
+    int savecounter = 0, it;
+    const char *name = method == NS3D_SIMPLER ? "SIMPLER" : method == NS3D_SIMPLERR ? "SIMPLER-R" : "IDEAL";
+    const char *maxname = method == NS3D_SIMPLER    ? "Max number of SIMPLE iterations: "
+                          : method == NS3D_SIMPLERR ? "Max number of SIMPLE-R iterations: "
+                                                    : "Max number of IDEAL iterations: ";
+    for (DBuf<double> *f : {&uh, &vh, &wh, &ut, &vt, &wt})
+        if (f->n) NS3D_CUDA_CHECK(cudaMemsetAsync(f->p, 0, f->n * 8, stream));
+    header(name, maxname);
+    initial_velocity(s);
+    alpha = alpha0;
+    for (it = 0; it < prm.maxitSIMPLE; ++it) {
+        info.s("Iteration ").i(it).s("  ------------").nl();
+        assemble_all_momentum();
+        d2d(ut.p, u.p, U.npad);
+        d2d(vt.p, v.p, V.npad);
+        if (nw > 0) d2d(wt.p, w.p, W.npad);
+        for (int sub = 0; sub < prm.N1; ++sub)
+            pressure_step(true, ut.p, vt.p, wt.p, u.p, v.p, w.p, ut.p, vt.p, wt.p);
+        compute_velocity_field(true, s.v_moy * std::min(1., alpha * 1.5));
+        diagnostics(s);
+        old_rmr_update(it);
+        if (method == NS3D_SIMPLER) res_row(it, s);
+        if (it > 1 && check_convergence(RMR, prm.simpletol)) {
+            info.s("Permeability K (m²): ").d(s.K).nl();
+            res.converged = 1;
+            break;
+        }
+        const Grid g = grid();
+        Phys ph = phys();
+        if (method == NS3D_SIMPLER || method == NS3D_SIMPLERR) {
+            launch_assemble_pressure(2, 0, g, ph, P.view(), U.view(), V.view(), W.view(), u.p, v.p, w.p, p.p, stream);
+            compute_pressure_correction();
+            const double dvmax = s.v_moy * 100;
+            launch_correct_velocity(0, 0, g, ph, U.view(), pc.p, u.p, dvmax, stream);
+            launch_correct_velocity(1, 0, g, ph, V.view(), pc.p, v.p, dvmax, stream);
+            if (nw > 0) launch_correct_velocity(2, 0, g, ph, W.view(), pc.p, w.p, dvmax, stream);
+            if (method == NS3D_SIMPLERR) {
+                hats(u.p, v.p, w.p, u.p, v.p, w.p);
+                launch_assemble_pressure(0, 1, g, ph, P.view(), U.view(), V.view(), W.view(), uh.p, vh.p, wh.p, p.p,
+                                         stream);
+                compute_pressure_field();
+            }
+        } else {
+            d2d(ut.p, u.p, U.npad);
+            d2d(vt.p, v.p, V.npad);
+            if (nw > 0) d2d(wt.p, w.p, W.npad);
+            for (int sub = 0; sub < prm.N2; ++sub)
+                pressure_step(false, u.p, v.p, w.p, ut.p, vt.p, wt.p, u.p, v.p, w.p);
+        }
+        Scalars after = s;
+        divergence(after);
+        s.MaxDeltaV = after.MaxDeltaV; s.normdiv = after.normdiv; s.velocityNorm = after.velocityNorm;
+        s.maxdiv = after.maxdiv;
+        if (method == NS3D_SIMPLERR) {
+            res_row(it, s);
+            relax_control(false);
+            save_snapshot(it, savecounter);
+        } else {
+            save_snapshot(it, savecounter);
+            relax_control(true);
+        }
+    }
+    finish(name, it, s, t0, start);
+}
+
+// ============================ C-ABI =========================================
+#define NS3D_TRY try {
+#define NS3D_CATCH                                                   \
+    }                                                                \
+    catch (const ApiError &e) {                                      \
+        return set_error(e.code, e.what());                          \
+    }                                                                \
+    catch (const CudaError &e) {                                     \
+        return set_error(NS3D_ERR_CUDA, e.what());                   \
+    }                                                                \
+    catch (const std::bad_alloc &) {                                 \
+        return set_error(NS3D_ERR_OOM, "host allocation failed");    \
+    }                                                                \
+    catch (const std::exception &e) {                                \
+        return set_error(NS3D_ERR_ARG, e.what());                    \
+    }
+
+static ns3d_handle *checked(ns3d_handle *h) {
+    if (!h) throw ApiError(NS3D_ERR_ARG, "NULL handle");
+    return h;
+}
+
+static void validate(const ns3d_params &p) {
+    if (p.dx <= 0 || p.mu <= 0 || p.rho <= 0) throw ApiError(NS3D_ERR_ARG, "dx, mu and rho must be > 0");
+    if (p.maxitsolver <= 0 || p.maxitSIMPLE <= 0 || p.save_step <= 0)
+        throw ApiError(NS3D_ERR_ARG, "maxitsolver, maxitSIMPLE and save_step must be > 0");
+    if (p.direction < 1 || p.direction > 3) throw ApiError(NS3D_ERR_ARG, "direction must be 1, 2 or 3");
+    if (p.border < 0) throw ApiError(NS3D_ERR_ARG, "border must be >= 0");
+    if (p.method < NS3D_SIMPLEC || p.method > NS3D_IDEAL) throw ApiError(NS3D_ERR_ARG, "unknown method");
+    if (p.precision != NS3D_FP64 && p.precision != NS3D_MIXED) throw ApiError(NS3D_ERR_ARG, "unknown precision");
+    if (p.N1 < 0 || p.N2 < 0) throw ApiError(NS3D_ERR_ARG, "N1 and N2 must be >= 0");
+}
+
+extern "C" {
+
+NS3D_API int ns3d_abi_version(void) { return NS3D_ABI_VERSION; }
+NS3D_API const char *ns3d_backend_name(void) { return "gb300"; }
+NS3D_API const char *ns3d_last_error(void) { return g_err.c_str(); }
+
+NS3D_API void ns3d_params_default(ns3d_params *p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof *p);
+    p->dx = 1.0; p->dy = -1.0; p->dz = -1.0;
+    p->mu = 1e-3; p->rho = 1e3; p->p0 = 1e5; p->gradp = 1e2;
+    p->alpha = 0.8; p->beta = 1.0;
+    p->vsolvertol = 1e-5; p->psolvertol = 1e-6; p->pcsolvertol = 1e-3;
+    p->simpletol = 1e-4; p->deltaRMR = 1e-4;
+    p->maxitsolver = 1000; p->maxitSIMPLE = 500; p->N1 = 2; p->N2 = 2; p->save_step = 20;
+    p->porevalue = 0; p->direction = 1; p->border = 0;
+    p->method = NS3D_SIMPLEC; p->precision = NS3D_FP64;
+}
+
+NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw, int32_t nx, int32_t ny, int32_t nz,
+                       ns3d_handle **out) {
+    NS3D_TRY
+    if (!params || !raw || !out) throw ApiError(NS3D_ERR_ARG, "ns3d_open: NULL argument");
+    if (nx <= 0 || ny <= 0 || nz <= 0) throw ApiError(NS3D_ERR_ARG, "ns3d_open: bad image size");
+    validate(*params);
+    std::unique_ptr<ns3d_handle> H(new ns3d_handle());
+    ns3d_handle &h = *H;
+    h.prm = *params;
+    if (h.prm.dy <= 0) h.prm.dy = h.prm.dx;
+    if (h.prm.dz <= 0) h.prm.dz = h.prm.dx;
+    if (h.prm.porevalue != 0 && h.prm.porevalue != 1) h.prm.porevalue = 0;
+    NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    h.build(raw, nx, ny, nz);
+    h.dx = h.prm.dx; h.dy = h.prm.dy; h.dz = h.prm.dz; h.mu = h.prm.mu; h.rho = h.prm.rho;
+    h.p0 = h.prm.p0; h.gradp = h.prm.gradp; h.border = h.prm.border; h.deltaRMR = h.prm.deltaRMR;
+    // constructor constants, src/NSBase.cxx:155-179
+    h.p1 = -h.gradp * (h.dx * h.nx) + h.p0;
+    if (h.p1 < 0) { h.p0 -= h.p1; h.p1 = 0; }
+    h.schemefactor = 0; h.min_alpha = 0.001; h.min_beta = 0.001; h.relax = 0.05;
+    h.speedup = h.relax * 0.5; h.maxconvdelta = 2.5;
+    h.alpha = h.alpha0 = h.prm.alpha;
+    h.beta = h.beta0 = h.prm.beta;
+    std::memset(&h.res, 0, sizeof h.res);
+    h.default_fields();
+    h.sync();
+    *out = H.release();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_get_sizes(const ns3d_handle *h, ns3d_sizes *s) {
+    if (!h || !s) return set_error(NS3D_ERR_ARG, "NULL argument");
+    s->nx = h->nx; s->ny = h->ny; s->nz = h->nz;
+    s->np = h->np; s->nu = h->nu; s->nv = h->nv; s->nw = h->nw; s->reserved = 0;
+    return NS3D_OK;
+}
+
+NS3D_API int ns3d_get_index_arrays(ns3d_handle *H, int32_t *pi, int32_t *ui, int32_t *vi, int32_t *wi) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (pi) NS3D_CUDA_CHECK(cudaMemcpyAsync(pi, h.pmap.p, h.pmap.n * 4, cudaMemcpyDeviceToHost, h.stream));
+    if (ui) NS3D_CUDA_CHECK(cudaMemcpyAsync(ui, h.umap.p, h.umap.n * 4, cudaMemcpyDeviceToHost, h.stream));
+    if (vi) NS3D_CUDA_CHECK(cudaMemcpyAsync(vi, h.vmap.p, h.vmap.n * 4, cudaMemcpyDeviceToHost, h.stream));
+    if (wi) NS3D_CUDA_CHECK(cudaMemcpyAsync(wi, h.wmap.p, h.wmap.n * 4, cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_set_initial_fields(ns3d_handle *H, const double *pimg, const double *uimg, const double *vimg,
+                                     const double *wimg) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    h.default_fields();
+    const long N = (long)h.nx * h.ny * h.nz, NU = (long)(h.nx + 1) * h.ny * h.nz;
+    DBuf<double> tmp;
+    tmp.alloc((size_t)NU);
+    auto put = [&](const double *src, const int *map, long cells, double *f) {
+        if (!src) return;
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(tmp.p, src, cells * 8, cudaMemcpyHostToDevice, h.stream));
+        launch_scatter_image(map, cells, tmp.p, f, h.stream);
+        h.sync();
+    };
+    put(pimg, h.pmap.p, N, h.p.p);
+    put(uimg, h.umap.p, NU, h.u.p);
+    put(vimg, h.vmap.p, N, h.v.p);
+    put(wimg, h.wmap.p, N, h.w.p);
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_get_fields(ns3d_handle *H, double *p, double *u, double *v, double *w) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (p) NS3D_CUDA_CHECK(cudaMemcpyAsync(p, h.p.p, (size_t)h.np * 8, cudaMemcpyDeviceToHost, h.stream));
+    if (u) NS3D_CUDA_CHECK(cudaMemcpyAsync(u, h.u.p, (size_t)h.nu * 8, cudaMemcpyDeviceToHost, h.stream));
+    if (v) NS3D_CUDA_CHECK(cudaMemcpyAsync(v, h.v.p, (size_t)h.nv * 8, cudaMemcpyDeviceToHost, h.stream));
+    if (w) NS3D_CUDA_CHECK(cudaMemcpyAsync(w, h.w.p, (size_t)h.nw * 8, cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_set_fields(ns3d_handle *H, const double *p, const double *u, const double *v, const double *w) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (p) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.p.p, p, (size_t)h.np * 8, cudaMemcpyHostToDevice, h.stream));
+    if (u) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.u.p, u, (size_t)h.nu * 8, cudaMemcpyHostToDevice, h.stream));
+    if (v) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.v.p, v, (size_t)h.nv * 8, cudaMemcpyHostToDevice, h.stream));
+    if (w) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.w.p, w, (size_t)h.nw * 8, cudaMemcpyHostToDevice, h.stream));
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_get_field_images(ns3d_handle *H, double *pimg, double *uimg, double *vimg, double *wimg,
+                                   double *vavg) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    const long N = (long)h.nx * h.ny * h.nz, NU = (long)(h.nx + 1) * h.ny * h.nz;
+    DBuf<double> tmp;
+    tmp.alloc((size_t)std::max(3 * N, NU));
+    auto get = [&](double *dst, const int *map, long cells, const double *f) {
+        if (!dst) return;
+        launch_gather_image(map, cells, f, tmp.p, h.stream);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(dst, tmp.p, cells * 8, cudaMemcpyDeviceToHost, h.stream));
+        h.sync();
+    };
+    get(pimg, h.pmap.p, N, h.p.p);
+    get(uimg, h.umap.p, NU, h.u.p);
+    get(vimg, h.vmap.p, N, h.v.p);
+    get(wimg, h.wmap.p, N, h.w.p);
+    if (vavg) {
+        launch_face_average(h.grid(), h.u.p, h.v.p, h.w.p, tmp.p, h.stream);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(vavg, tmp.p, 3 * N * 8, cudaMemcpyDeviceToHost, h.stream));
+        h.sync();
+    }
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, int32_t write_fields) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    h.info.close();
+    h.resl.close();
+    h.have_out = false;
+    if (!dir) return NS3D_OK;
+    h.outdir = dir;
+    h.stem = stem ? stem : "image";
+    h.write_fields = write_fields != 0;
+    std::string d = h.outdir.empty() ? std::string() : h.outdir + "/";
+    std::string tag = std::to_string(h.prm.direction) + "-" + h.stem;
+    if (!h.info.open(d + "INFO-" + tag + ".log", 15) || !h.resl.open(d + "RES-" + tag + ".csv", 6))
+        throw ApiError(NS3D_ERR_IO, std::string("cannot open log files in ") + dir);
+    h.have_out = true;
+    // the constructor lines that reach the INFO file, src/NSBase.cxx:143,182-187
+    h.info.s("Size ").i(h.nx).s(",").i(h.ny).s(",").i(h.nz).nl();
+    h.info.s("Porosity: ").d((double)(float(h.np) / float((long)h.nx * h.ny * h.nz))).nl();
+    h.info.s("Nodes for the pressure field: ").i(h.np).nl();
+    h.info.s("Nodes for the u velocity field: ").i(h.nu).nl();
+    h.info.s("Nodes for the v velocity field: ").i(h.nv).nl();
+    h.info.s("Nodes for the w velocity field: ").i(h.nw).nl();
+    h.info.s("Delta RMR min : ").d(h.deltaRMR).nl();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_solve(ns3d_handle *H) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (h.prm.precision != NS3D_FP64) throw ApiError(NS3D_ERR_UNSUPPORTED, "mixed precision is not built yet");
+    std::memset(&h.res, 0, sizeof h.res);
+    h.su = h.sv = h.sw = h.sp = SolveOutcome();
+    h.alpha = h.alpha0;
+    h.beta = h.beta0;
+    h.avgRMR.clear();
+    h.RMR = h.old_RMR = 0;
+    h.kmom.reset_launch_count();
+    h.kp.reset_launch_count();
+    if (h.prm.method == NS3D_SIMPLEC) h.run_simplec();
+    else h.run_simpler_family(h.prm.method);
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_get_result(const ns3d_handle *h, ns3d_result *r) {
+    if (!h || !r) return set_error(NS3D_ERR_ARG, "NULL argument");
+    *r = h->res;
+    return NS3D_OK;
+}
+
+NS3D_API int ns3d_assemble_momentum(ns3d_handle *H) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    h.assemble_all_momentum();
+    h.momentum_rhs();
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_assemble_pressure_correction(ns3d_handle *H, int32_t simplec) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    launch_assemble_pressure(simplec ? 1 : 2, 0, h.grid(), h.phys(), h.P.view(), h.U.view(), h.V.view(), h.W.view(),
+                             h.u.p, h.v.p, h.w.p, h.p.p, h.stream);
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_assemble_pressure(ns3d_handle *H, int32_t relax) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    h.hats(h.u.p, h.v.p, h.w.p, h.u.p, h.v.p, h.w.p);
+    launch_assemble_pressure(0, relax ? 1 : 0, h.grid(), h.phys(), h.P.view(), h.U.view(), h.V.view(), h.W.view(),
+                             h.uh.p, h.vh.p, h.wh.p, h.p.p, h.stream);
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+static DevSys *sys_of(ns3d_handle &h, int sys) {
+    switch (sys) {
+        case NS3D_SYS_U: return &h.U;
+        case NS3D_SYS_V: return &h.V;
+        case NS3D_SYS_W: return &h.W;
+        case NS3D_SYS_P: return &h.P;
+        default: throw ApiError(NS3D_ERR_ARG, "bad system index");
+    }
+}
+
+NS3D_API int ns3d_get_system(ns3d_handle *H, int32_t sys, double *coef, int32_t *nbr, double *rhs, double *rowsum) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    DevSys &S = *sys_of(h, sys);
+    const size_t n = (size_t)S.n;
+    for (int s = 0; s < 7 && coef; ++s)
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(coef + s * n, S.coef.p + (size_t)s * S.npad, n * 8, cudaMemcpyDeviceToHost,
+                                        h.stream));
+    for (int s = 0; s < 6 && nbr; ++s)
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(nbr + s * n, S.nbr.p + (size_t)s * S.npad, n * 4, cudaMemcpyDeviceToHost,
+                                        h.stream));
+    if (rhs) NS3D_CUDA_CHECK(cudaMemcpyAsync(rhs, S.rhs.p, n * 8, cudaMemcpyDeviceToHost, h.stream));
+    if (rowsum) NS3D_CUDA_CHECK(cudaMemcpyAsync(rowsum, S.rowsum.p, n * 8, cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_solve_system(ns3d_handle *H, int32_t sys, const double *rhs, double *x, double tol, int32_t maxit,
+                               ns3d_solve_info *info) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (!x || maxit <= 0) throw ApiError(NS3D_ERR_ARG, "ns3d_solve_system: bad argument");
+    DevSys &S = *sys_of(h, sys);
+    DBuf<double> dx, db;
+    dx.alloc_zero(S.npad, h.stream);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(dx.p, x, (size_t)S.n * 8, cudaMemcpyHostToDevice, h.stream));
+    const double *b = S.rhs.p;
+    if (rhs) {
+        db.alloc_zero(S.npad, h.stream);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(db.p, rhs, (size_t)S.n * 8, cudaMemcpyHostToDevice, h.stream));
+        b = db.p;
+    }
+    KrylovSet ks;
+    std::vector<SolveOutcome> out;
+    ks.run({{&S, dx.p, b, tol, maxit}}, h.stream, out);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(x, dx.p, (size_t)S.n * 8, cudaMemcpyDeviceToHost, h.stream));
+    h.sync();
+    if (info) {
+        info->iterations = out[0].iters;
+        info->info = out[0].info;
+        info->error = out[0].error;
+    }
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_close(ns3d_handle *h) {
+    delete h;
+    return NS3D_OK;
+}
+
+}  // extern "C"
