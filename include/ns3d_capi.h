@@ -227,6 +227,19 @@ NS3D_API int ns3d_solve_system(ns3d_handle *h, int32_t sys, const double *rhs, d
 
 NS3D_API int ns3d_close(ns3d_handle *h);
 
+/* ---- measurement (no counterpart in the reference, which only times whole
+ * solves with time(0), src/SIMPLEC.cxx:59,228-231) -------------------------- */
+/* per-kernel device time of the pressure(-correction) BiCGSTAB kernels,
+ * collected with CUDA events on the solver's stream while enabled */
+typedef struct ns3d_profile {
+    int64_t launches[6];      /* K1 p-update, K2 SpMV+dot, K3 s-update, K4 SpMV+dots, K5 x/r-update, init */
+    double ms[6];             /* summed device milliseconds per kernel */
+    int64_t rows[6];          /* summed rows processed (active systems only) */
+    int64_t total_launches;   /* every kernel launched by this handle */
+} ns3d_profile;
+NS3D_API int ns3d_set_profiling(ns3d_handle *h, int32_t enable);
+NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
+
 /* ---- host utilities (CUDA library only; no device work) ----------------- */
 /*
  * Parse an ini file like ReadInput (src/navierstokes3D.cxx:266-463): same

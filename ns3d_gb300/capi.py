@@ -46,6 +46,11 @@ class Result(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class Profile(C.Structure):
+    _fields_ = [("launches", C.c_int64 * 6), ("ms", C.c_double * 6), ("rows", C.c_int64 * 6),
+                ("total_launches", C.c_int64)]
+
+
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("info", C.c_int32), ("error", C.c_double)]
 
@@ -84,6 +89,9 @@ def _declare(lib):
         "ns3d_solve_system": (C.c_int, [C.c_void_p, C.c_int32, _d, _d, C.c_double, C.c_int32, _P(SolveInfo)]),
         "ns3d_close": (C.c_int, [C.c_void_p]),
     }
+    if hasattr(lib, "ns3d_set_profiling"):
+        sig["ns3d_set_profiling"] = (C.c_int, [C.c_void_p, C.c_int32])
+        sig["ns3d_get_profile"] = (C.c_int, [C.c_void_p, _P(Profile)])
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res
@@ -215,6 +223,14 @@ class Solver:
         self._check(self.lib.ns3d_solve_system(self.h, sys, _ptr(b, C.c_double), _ptr(x, C.c_double),
                                                float(tol), int(maxit), C.byref(info)))
         return x, info
+
+    def set_profiling(self, enable=True):
+        self._check(self.lib.ns3d_set_profiling(self.h, int(bool(enable))))
+
+    def profile(self):
+        p = Profile()
+        self._check(self.lib.ns3d_get_profile(self.h, C.byref(p)))
+        return p
 
     def close(self):
         if getattr(self, "h", None):

@@ -69,7 +69,8 @@ struct SysView {
 template <class Op>
 __device__ __forceinline__ double row_ordered(int row, int nW, int nE, int nS, int nN, int nB, int nT, Op op) {
     double acc = 0.0;
-    if (nW == row - 1) {
+    // nW >= 0 matters for row 0: a missing W (-1) must not read as "row - 1"
+    if (nW >= 0 && nW == row - 1) {
         if (nS >= 0) acc = op(acc, SS, nS);
         if (nB >= 0) acc = op(acc, SB, nB);
         acc = op(acc, SW, nW);
@@ -79,7 +80,7 @@ __device__ __forceinline__ double row_ordered(int row, int nW, int nE, int nS, i
         if (nB >= 0) acc = op(acc, SB, nB);
     }
     acc = op(acc, SP, row);
-    if (nE == row + 1) {
+    if (nE >= 0 && nE == row + 1) {
         acc = op(acc, SE, nE);
         if (nT >= 0) acc = op(acc, ST, nT);
         if (nN >= 0) acc = op(acc, SN, nN);

@@ -229,16 +229,16 @@ void launch_build_image(const uint8_t *raw, int rnx, int rny, int rnz, int dir, 
                         int nx, int ny, int nz, cudaStream_t st) {
     long N = (long)nx * ny * nz;
     int grid = (int)std::min<long>((N + 255) / 256, 152L * 64);
-    k_build_image<<<grid, 256, 0, st>>>(raw, rnx, rny, rnz, dir, border, (uint8_t)pv, img, nx, ny, nz);
+    count_launches(1); k_build_image<<<grid, 256, 0, st>>>(raw, rnx, rny, rnz, dir, border, (uint8_t)pv, img, nx, ny, nz);
 }
 
 void launch_index_build(const uint8_t *img, int nx, int ny, int nz, int4 *blk, int4 *totals, int *pmap, int *umap,
                         int *vmap, int *wmap, int *pcell, int *ucell, int *vcell, int *wcell, cudaStream_t st) {
     long N = (long)nx * ny * nz;
     int nblk = (int)((N + GEO_CELLS - 1) / GEO_CELLS);
-    k_count<<<nblk, GEO_THREADS, 0, st>>>(img, nx, ny, nz, blk);
-    k_scan_blocks<<<1, GEO_THREADS, 0, st>>>(blk, nblk, totals);
-    k_scatter<<<nblk, GEO_THREADS, 0, st>>>(img, nx, ny, nz, blk, pmap, umap, vmap, wmap, pcell, ucell, vcell, wcell);
+    count_launches(1); k_count<<<nblk, GEO_THREADS, 0, st>>>(img, nx, ny, nz, blk);
+    count_launches(1); k_scan_blocks<<<1, GEO_THREADS, 0, st>>>(blk, nblk, totals);
+    count_launches(1); k_scatter<<<nblk, GEO_THREADS, 0, st>>>(img, nx, ny, nz, blk, pmap, umap, vmap, wmap, pcell, ucell, vcell, wcell);
 }
 
 int index_build_blocks(long ncells) { return (int)((ncells + GEO_CELLS - 1) / GEO_CELLS); }
@@ -247,13 +247,13 @@ void launch_nbr_mom(const int *map, int d0, int ny, int nz, const int *cell, int
                     cudaStream_t st) {
     if (n <= 0) return;
     int grid = std::min((n + 255) / 256, 152 * 32);
-    k_nbr_mom<<<grid, 256, 0, st>>>(map, d0, ny, nz, cell, n, npad, nbr, zdir);
+    count_launches(1); k_nbr_mom<<<grid, 256, 0, st>>>(map, d0, ny, nz, cell, n, npad, nbr, zdir);
 }
 
 void launch_nbr_p(const Grid &g, const int *cell, int n, int npad, int *nbr, cudaStream_t st) {
     if (n <= 0) return;
     int grid = std::min((n + 255) / 256, 152 * 32);
-    k_nbr_p<<<grid, 256, 0, st>>>(g, cell, n, npad, nbr);
+    count_launches(1); k_nbr_p<<<grid, 256, 0, st>>>(g, cell, n, npad, nbr);
 }
 
 }  // namespace ns3d

@@ -76,5 +76,11 @@ void launch_krylov_iteration(const KSys *sys, int nsys, const int *chunk_sys, in
 void launch_krylov_restart(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st);
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st);
 int device_sm_count();
+// K1..K5 of one BiCGSTAB iteration launched one at a time (profiling)
+void launch_krylov_kernel(int which, const KSys *sys, int nsys, const int *chunk_sys, int total_chunks,
+                          cudaStream_t st);
+// kernels launched by this library since it was loaded
+int64_t launch_count();
+void count_launches(int64_t n);
 
 }  // namespace ns3d

@@ -23,6 +23,7 @@
 //   K5 x += alpha y + w z; r = s - w t, <r0,r>, <r,r> -> convergence, beta
 // No kernel waits on another block: completion is detected with one atomic
 // counter per system, so every launch terminates on its own.
+#include <atomic>
 #include <cfloat>
 
 #include "device.cuh"
@@ -430,6 +431,10 @@ __global__ void k_spmv(SysView A, const double *__restrict__ x, double *__restri
     }
 }
 
+static std::atomic<int64_t> g_launches{0};
+int64_t launch_count() { return g_launches.load(); }
+void count_launches(int64_t n) { g_launches += n; }
+
 static int g_sms = 0;
 int device_sm_count() {
     if (g_sms == 0) {
@@ -446,30 +451,45 @@ static inline int kr_grid(int total_chunks) { return std::max(1, std::min(total_
 void launch_krylov_init(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
     (void)nsys;
     if (total_chunks <= 0) return;
-    k_kr_init<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_kr_init2<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_init<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_init2<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
 }
 
 void launch_krylov_iteration(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
     (void)nsys;
     if (total_chunks <= 0) return;
     const int g = kr_grid(total_chunks);
-    k_kr_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_kr_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_kr_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_kr_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_kr_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+}
+
+void launch_krylov_kernel(int which, const KSys *sys, int nsys, const int *chunk_sys, int total_chunks,
+                          cudaStream_t st) {
+    (void)nsys;
+    if (total_chunks <= 0) return;
+    const int g = kr_grid(total_chunks);
+    count_launches(1);
+    switch (which) {
+        case 0: k_kr_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+        case 1: k_kr_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+        case 2: k_kr_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+        case 3: k_kr_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+        default: k_kr_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+    }
 }
 
 void launch_krylov_restart(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
     (void)nsys;
     if (total_chunks <= 0) return;
-    k_kr_restart<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    count_launches(1); k_kr_restart<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
 }
 
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st) {
     if (A.n <= 0) return;
-    k_spmv<<<std::max(1, std::min(A.nchunks, device_sm_count() * 6)), LANES, 0, st>>>(A, x, y);
+    count_launches(1); k_spmv<<<std::max(1, std::min(A.nchunks, device_sm_count() * 6)), LANES, 0, st>>>(A, x, y);
 }
 
 }  // namespace ns3d

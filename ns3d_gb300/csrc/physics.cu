@@ -885,23 +885,23 @@ static inline int chunk_grid(int nch) { return std::max(1, std::min(nch, 152 * 8
 void launch_assemble_momentum(int comp, const Grid &g, const Phys &ph, const SysView &A, const double *uc,
                               const double *vc, const double *wc, cudaStream_t st) {
     if (A.n <= 0) return;
-    if (comp == 0) k_mom_x<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc);
-    else if (comp == 1) k_mom_y<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc);
-    else k_mom_z<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc);
+    if (comp == 0) { count_launches(1); k_mom_x<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc); }
+    else if (comp == 1) { count_launches(1); k_mom_y<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc); }
+    else { count_launches(1); k_mom_z<<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, uc, vc, wc); }
 }
 
 void launch_momentum_rhs(int comp, const Grid &g, const Phys &ph, const SysView &A, const double *p,
                          const double *x, cudaStream_t st) {
     if (A.n <= 0) return;
-    if (comp == 0) k_mom_rhs<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x);
-    else if (comp == 1) k_mom_rhs<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x);
-    else k_mom_rhs<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x);
+    if (comp == 0) { count_launches(1); k_mom_rhs<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x); }
+    else if (comp == 1) { count_launches(1); k_mom_rhs<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x); }
+    else { count_launches(1); k_mom_rhs<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, x); }
 }
 
 void launch_hat(const SysView &A, const Phys &ph, const double *xc, const double *xold, double *hat,
                 cudaStream_t st) {
     if (A.n <= 0) return;
-    k_hat<<<rows_grid(A.n), 256, 0, st>>>(A, ph, xc, xold, hat);
+    count_launches(1); k_hat<<<rows_grid(A.n), 256, 0, st>>>(A, ph, xc, xold, hat);
 }
 
 void launch_assemble_pressure(int mode, int relax, const Grid &g, const Phys &ph, const SysView &S,
@@ -911,37 +911,37 @@ void launch_assemble_pressure(int mode, int relax, const Grid &g, const Phys &ph
     const double *au = (mode == 1) ? U.rowsum : U.coef;  // slot P is the first slot
     const double *av = (mode == 1) ? V.rowsum : V.coef;
     const double *aw = (mode == 1) ? W.rowsum : W.coef;
-    k_pressure<<<rows_grid(S.n), 256, 0, st>>>(mode, relax, g, ph, S, au, av, aw, uc, vc, wc, p);
+    count_launches(1); k_pressure<<<rows_grid(S.n), 256, 0, st>>>(mode, relax, g, ph, S, au, av, aw, uc, vc, wc, p);
 }
 
 void launch_correct_velocity(int comp, int simplec, const Grid &g, const Phys &ph, const SysView &A,
                              const double *pc, double *x, double dvmax, cudaStream_t st) {
     if (A.n <= 0) return;
     const double *den = simplec ? A.rowsum : A.coef;
-    if (comp == 0) k_correct<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax);
-    else if (comp == 1) k_correct<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax);
-    else k_correct<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax);
+    if (comp == 0) { count_launches(1); k_correct<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax); }
+    else if (comp == 1) { count_launches(1); k_correct<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax); }
+    else { count_launches(1); k_correct<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, den, pc, x, dvmax); }
 }
 
 void launch_correct_velocity_simpler(int comp, const Grid &g, const Phys &ph, const SysView &A, const double *p,
                                      const double *hat, double *x, double p_0, double p_1, cudaStream_t st) {
     if (A.n <= 0) return;
-    if (comp == 0) k_correct_simpler<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1);
-    else if (comp == 1) k_correct_simpler<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1);
-    else k_correct_simpler<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1);
+    if (comp == 0) { count_launches(1); k_correct_simpler<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
+    else if (comp == 1) { count_launches(1); k_correct_simpler<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
+    else { count_launches(1); k_correct_simpler<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
 }
 
 void launch_velocity_post(const double *temp, double *x, int n, const KState *st_dev, int limit, double dvmax,
                           cudaStream_t st) {
     if (n <= 0) return;
-    k_velocity_post<<<rows_grid(n), 256, 0, st>>>(temp, x, n, st_dev, limit, dvmax);
+    count_launches(1); k_velocity_post<<<rows_grid(n), 256, 0, st>>>(temp, x, n, st_dev, limit, dvmax);
 }
 
 void launch_permeability(const Grid &g, const double *u, const double *p, int border, double *part, DiagOut *out,
                          cudaStream_t st) {
     long plane = (long)g.ny * g.nz;
     int nch = (int)((plane + CH - 1) / CH);
-    k_permeability<<<chunk_grid(nch), LANES, 0, st>>>(g, u, p, border, part, out);
+    count_launches(1); k_permeability<<<chunk_grid(nch), LANES, 0, st>>>(g, u, p, border, part, out);
 }
 
 void launch_divergence(const Grid &g, const Phys &ph, const SysView &P, const double *u, const double *v,
@@ -950,30 +950,30 @@ void launch_divergence(const Grid &g, const Phys &ph, const SysView &P, const do
         cudaMemsetAsync(&out->maxdv, 0, 4 * sizeof(double), st);
         return;
     }
-    k_divergence<<<chunk_grid(P.nchunks), LANES, 0, st>>>(g, ph, P, u, v, w, part, out);
+    count_launches(1); k_divergence<<<chunk_grid(P.nchunks), LANES, 0, st>>>(g, ph, P, u, v, w, part, out);
 }
 
 void launch_correct_pressure(const SysView &P, const double *pc, double *p, double beta, double *part,
                              DiagOut *out, cudaStream_t st) {
     if (P.n <= 0) return;
-    k_correct_pressure<<<chunk_grid(P.nchunks), LANES, 0, st>>>(P, pc, p, beta, part, out);
+    count_launches(1); k_correct_pressure<<<chunk_grid(P.nchunks), LANES, 0, st>>>(P, pc, p, beta, part, out);
 }
 
 void launch_default_pressure(const Grid &g, const SysView &P, double p0, double p1, double *p, cudaStream_t st) {
     if (P.n <= 0) return;
-    k_default_pressure<<<rows_grid(P.n), 256, 0, st>>>(g, P, p0, p1, p);
+    count_launches(1); k_default_pressure<<<rows_grid(P.n), 256, 0, st>>>(g, P, p0, p1, p);
 }
 
 void launch_gather_image(const int *map, long ncells, const double *field, double *img, cudaStream_t st) {
-    k_gather_image<<<rows_grid(ncells), 256, 0, st>>>(map, ncells, field, img);
+    count_launches(1); k_gather_image<<<rows_grid(ncells), 256, 0, st>>>(map, ncells, field, img);
 }
 void launch_scatter_image(const int *map, long ncells, const double *img, double *field, cudaStream_t st) {
-    k_scatter_image<<<rows_grid(ncells), 256, 0, st>>>(map, ncells, img, field);
+    count_launches(1); k_scatter_image<<<rows_grid(ncells), 256, 0, st>>>(map, ncells, img, field);
 }
 void launch_face_average(const Grid &g, const double *u, const double *v, const double *w, double *vavg,
                          cudaStream_t st) {
     long N = (long)g.nx * g.ny * g.nz;
-    k_face_average<<<rows_grid(N), 256, 0, st>>>(g, u, v, w, vavg);
+    count_launches(1); k_face_average<<<rows_grid(N), 256, 0, st>>>(g, u, v, w, vavg);
 }
 
 }  // namespace ns3d

@@ -125,8 +125,21 @@ class KrylovSet {
     long launches() const { return launches_; }
     void reset_launch_count() { launches_ = 0; }
 
+    // per-kernel CUDA-event timing of K1..K5 (index 0..4) and init (5)
+    struct Profile {
+        int64_t launches[6] = {0, 0, 0, 0, 0, 0};
+        double ms[6] = {0, 0, 0, 0, 0, 0};
+        int64_t rows[6] = {0, 0, 0, 0, 0, 0};
+    };
+    bool profiling = false;
+    Profile prof;
+    ~KrylovSet();
+
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
+    void issue_batch(int batch, cudaStream_t st);
+    void collect_batch(int batch, const std::vector<int> &work_before);
+    std::vector<cudaEvent_t> events_;
     DBuf<KSys> ksys_;
     DBuf<int> chunk_sys_;
     DBuf<KState> st_;

@@ -125,14 +125,17 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
     const long cap = 2L * maxit + 64;
     long issued = 0;
     int batch = std::max(1, std::min(32, prev_iters_ / 2));
-    int max_iters = 0;
+    int max_iters = 0, last_batch = 0;
+    std::vector<int> work_before(ns, 0);
     while (true) {
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (profiling && last_batch > 0) collect_batch(last_batch, work_before);
         bool all_done = true, any_paused = false;
         for (int i = 0; i < ns; ++i) {
             if (!h_st_.p[i].done) all_done = false;
             if (h_st_.p[i].paused && !h_st_.p[i].done) any_paused = true;
+            work_before[i] = h_st_.p[i].work;
         }
         if (all_done) break;
         if (issued >= cap) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
@@ -140,7 +143,8 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
             launch_krylov_restart(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
             launches_ += 1;
         }
-        for (int b = 0; b < batch; ++b) launch_krylov_iteration(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+        issue_batch(batch, st);
+        last_batch = batch;
         launches_ += 5L * batch;
         issued += batch;
         batch = std::min(64, batch * 2);
@@ -155,6 +159,44 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
         if (!k.zero_rhs) max_iters = std::max(max_iters, k.work);
     }
     prev_iters_ = std::max(2, max_iters);
+}
+
+KrylovSet::~KrylovSet() {
+    for (cudaEvent_t e : events_) cudaEventDestroy(e);
+}
+
+void KrylovSet::issue_batch(int batch, cudaStream_t st) {
+    if (!profiling) {
+        for (int b = 0; b < batch; ++b) launch_krylov_iteration(ksys_.p, nsys_, chunk_sys_.p, total_chunks_, st);
+        return;
+    }
+    const size_t need = (size_t)batch * 5 + 1;
+    while (events_.size() < need) {
+        cudaEvent_t e;
+        NS3D_CUDA_CHECK(cudaEventCreate(&e));
+        events_.push_back(e);
+    }
+    NS3D_CUDA_CHECK(cudaEventRecord(events_[0], st));
+    for (int b = 0; b < batch; ++b)
+        for (int k = 0; k < 5; ++k) {
+            launch_krylov_kernel(k, ksys_.p, nsys_, chunk_sys_.p, total_chunks_, st);
+            NS3D_CUDA_CHECK(cudaEventRecord(events_[(size_t)b * 5 + k + 1], st));
+        }
+}
+
+void KrylovSet::collect_batch(int batch, const std::vector<int> &work_before) {
+    for (int b = 0; b < batch; ++b) {
+        int64_t rows = 0;
+        for (int i = 0; i < nsys_; ++i)
+            if (h_st_.p[i].work - work_before[i] > b) rows += cur_[i].n;
+        for (int k = 0; k < 5; ++k) {
+            float ms = 0;
+            NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, events_[(size_t)b * 5 + k], events_[(size_t)b * 5 + k + 1]));
+            prof.ms[k] += ms;
+            prof.launches[k] += 1;
+            prof.rows[k] += rows;
+        }
+    }
 }
 
 // ============================ solver instance ================================
@@ -1066,6 +1108,32 @@ NS3D_API int ns3d_solve_system(ns3d_handle *H, int32_t sys, const double *rhs, d
 NS3D_API int ns3d_close(ns3d_handle *h) {
     delete h;
     return NS3D_OK;
+}
+
+static int64_t g_launch_base = 0;
+
+NS3D_API int ns3d_set_profiling(ns3d_handle *H, int32_t enable) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    h.kp.profiling = enable != 0;
+    h.kp.prof = KrylovSet::Profile();
+    g_launch_base = launch_count();
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_get_profile(ns3d_handle *H, ns3d_profile *out) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (!out) throw ApiError(NS3D_ERR_ARG, "NULL profile");
+    for (int k = 0; k < 6; ++k) {
+        out->launches[k] = h.kp.prof.launches[k];
+        out->ms[k] = h.kp.prof.ms[k];
+        out->rows[k] = h.kp.prof.rows[k];
+    }
+    out->total_launches = launch_count() - g_launch_base;
+    return NS3D_OK;
+    NS3D_CATCH
 }
 
 }  // extern "C"

@@ -201,6 +201,7 @@ struct System {
 
 struct SolveOut {
     long iters = 0;
+    long work = 0;  // iterations executed, restarts included
     double error = 0.0;
     int info = NS3D_SUCCESS;
     bool valid = false;
@@ -281,6 +282,7 @@ SolveOut bicgstab(const System &A, const std::vector<double> &b, std::vector<dou
         }
         rr = det_dot(r, r, n);
         ++i;
+        ++out.work;
         if (krylov_rows) *krylov_rows += n;
     }
     out.iters = i;
@@ -1110,7 +1112,7 @@ void velocity_component(Handle &h, System &A, std::vector<double> &x, void (*rhs
     rhs(h);
     std::vector<double> temp = x;
     so = bicgstab(A, A.rhs, x, h.prm.vsolvertol, h.prm.maxitsolver, &h.res.krylov_rows);
-    h.res.krylov_iterations += so.iters;
+    h.res.krylov_iterations += so.work;
     if (so.iters == 0 || so.info != 0) x = temp;
     if (limit) {
 #pragma omp parallel for schedule(static)
@@ -1153,7 +1155,7 @@ void log_pressure_status(Handle &h, const SolveOut &o) {
 void compute_pressure_correction(Handle &h) {
     h.info.s("Solving for pressure correction : ");
     h.sp = bicgstab(h.P, h.P.rhs, h.pc, h.prm.pcsolvertol, h.prm.maxitsolver, &h.res.krylov_rows);
-    h.res.krylov_iterations += h.sp.iters;
+    h.res.krylov_iterations += h.sp.work;
     log_pressure_status(h, h.sp);
 }
 
@@ -1162,11 +1164,11 @@ void compute_pressure_field(Handle &h) {
     h.info.s("Solving for pressure in : ");
     std::vector<double> ptemp = h.p;
     h.sp = bicgstab(h.P, h.P.rhs, ptemp, tol, h.prm.maxitsolver, &h.res.krylov_rows);
-    h.res.krylov_iterations += h.sp.iters;
+    h.res.krylov_iterations += h.sp.work;
     while (h.sp.iters == 0 && h.sp.info == NS3D_SUCCESS && tol > 1e-15) {
         tol *= 0.1;
         h.sp = bicgstab(h.P, h.P.rhs, ptemp, tol, h.prm.maxitsolver, &h.res.krylov_rows);
-        h.res.krylov_iterations += h.sp.iters;
+        h.res.krylov_iterations += h.sp.work;
     }
     if (h.sp.iters > 0) h.p = ptemp;
     log_pressure_status(h, h.sp);

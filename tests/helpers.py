@@ -22,7 +22,7 @@ def params(lib, **kw):
     return capi.default_params(lib, **base)
 
 
-def test_spheres_params(lib, **kw):
+def spheres_params(lib, **kw):
     """Parameters of the reference's tests/test_spheres.ini and compare_algorithms.ini."""
     base = dict(dx=2e-6, dy=-1, dz=-1, mu=1e-3, rho=1e3, p0=1e5, gradp=1e2, alpha=0.8, beta=1.0,
                 vsolvertol=1e-5, psolvertol=1e-6, pcsolvertol=1e-3, simpletol=1e-4, maxitsolver=500,

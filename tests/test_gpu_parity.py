@@ -9,7 +9,7 @@ tolerances are asserted too, so a failure says which bar broke.
 import numpy as np
 import pytest
 
-from helpers import params, rel_l2, solver, test_spheres_params
+from helpers import params, rel_l2, solver, spheres_params
 from ns3d_gb300 import capi, synth
 
 pytestmark = pytest.mark.gpu
@@ -54,8 +54,8 @@ def test_index_arrays_bit_exact(gpulib, oracle, case):
 
 def test_index_arrays_lattice_128(gpulib, oracle):
     img = synth.sphere_lattice(128, 12, 5)
-    g = solver(gpulib, img, test_spheres_params(gpulib))
-    o = solver(oracle, img, test_spheres_params(oracle))
+    g = solver(gpulib, img, spheres_params(gpulib))
+    o = solver(oracle, img, spheres_params(oracle))
     assert (g.sizes.np, g.sizes.nu, g.sizes.nv, g.sizes.nw) == (1582152, 1517536, 1484768, 1484768)
     for a, b in zip(g.index_arrays(), o.index_arrays()):
         assert np.array_equal(a, b)
@@ -181,8 +181,8 @@ def test_golden_config_first_iterations(gpulib, oracle, tmp_path):
     (tmp_path / "g").mkdir()
     (tmp_path / "o").mkdir()
     img = synth.sphere_lattice(128, 12, 5)
-    g = solver(gpulib, img, test_spheres_params(gpulib, maxitSIMPLE=3))
-    o = solver(oracle, img, test_spheres_params(oracle, maxitSIMPLE=3))
+    g = solver(gpulib, img, spheres_params(gpulib, maxitSIMPLE=3))
+    o = solver(oracle, img, spheres_params(oracle, maxitSIMPLE=3))
     _compare_solves(g, o, tmp_path)
 
 

@@ -6,7 +6,7 @@ import hashlib
 import numpy as np
 import pytest
 
-from helpers import golden, solver, test_spheres_params
+from helpers import golden, solver, spheres_params
 from ns3d_gb300 import synth
 
 LATTICES = {"spheres_64.vti": (64, 8, 3), "spheres_128.vti": (128, 12, 5)}
@@ -23,7 +23,7 @@ def test_lattice_generator_reproduces_reference_images(name):
 
 def test_index_counts_and_porosity_128(oracle):
     img = synth.sphere_lattice(128, 12, 5)
-    s = solver(oracle, img, test_spheres_params(oracle))
+    s = solver(oracle, img, spheres_params(oracle))
     g = golden()
     assert dict(np=s.sizes.np, nu=s.sizes.nu, nv=s.sizes.nv, nw=s.sizes.nw) == g["info_counts"]
     por = np.float32(s.sizes.np) / np.float32(128 ** 3)
@@ -35,7 +35,7 @@ def test_first_outer_iteration_matches_golden_run(oracle, tmp_path):
     every RES column of row 0 (6 digits) and the INFO head; the initial K to
     1e-12 relative (the golden log prints 15 digits)."""
     img = synth.sphere_lattice(128, 12, 5)
-    s = solver(oracle, img, test_spheres_params(oracle, maxitSIMPLE=1))
+    s = solver(oracle, img, spheres_params(oracle, maxitSIMPLE=1))
     s.set_output(tmp_path, "spheres_128", False)
     s.solve()
     s.close()
@@ -54,6 +54,8 @@ def test_first_outer_iteration_matches_golden_run(oracle, tmp_path):
         if b.startswith("Initial Permeability"):
             ka, kb = float(a.split(":")[1]), float(b.split(":")[1])
             assert abs(ka - kb) / kb < 1e-12
+        elif b.startswith("Max number of SIMPLE iterations"):
+            assert a == "Max number of SIMPLE iterations: 1"  # this run stops after one iteration
         else:
             assert a == b
 
@@ -65,7 +67,7 @@ def test_readme_64_table(oracle, method):
     are reproduced exactly.  SIMPLER's RMR sits on a plateau near simpletol,
     where rounding moves the crossing (30 here, 42 in the README)."""
     img = synth.sphere_lattice(64, 8, 3)
-    s = solver(oracle, img, test_spheres_params(oracle, maxitSIMPLE=200, method=method))
+    s = solver(oracle, img, spheres_params(oracle, maxitSIMPLE=200, method=method))
     r = s.solve()
     s.close()
     t = golden()["readme_64_table"][method]
