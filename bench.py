@@ -48,14 +48,16 @@ SPMV_BYTES_PER_ROW = 104  # 7*8 coefficients + 6*4 indices + 8 gathered x + 8 do
 # BiCGSTAB row-iterations of one complete solve of this workload per method,
 # measured by this benchmark's GPU arm; the CPU oracle follows the same
 # trajectory bit for bit, so these scale its sampled cost to a full solve.
-FULL_SOLVE_KRYLOV_ROWS = {}
+FULL_SOLVE_KRYLOV_ROWS = {"SIMPLEC": 246125574149, "SIMPLER": 316246186905, "SIMPLERR": 325991783660,
+                          "IDEAL": 87945733905}
+MAX_OUTER = 2000
 
 
 def workload_params(capi, lib, method):
     dx = 1e-6
     return capi.default_params(lib, dx=dx, dy=-1.0, dz=-1.0, mu=1e-3, rho=1.0, p0=1.0, gradp=1.0 / (SHAPE[0] * dx),
                                alpha=0.5, beta=1.0, vsolvertol=1e-8, psolvertol=1e-8, pcsolvertol=1e-8,
-                               simpletol=1e-6, maxitsolver=2000, maxitSIMPLE=2000, N1=2, N2=2, porevalue=0,
+                               simpletol=1e-6, maxitsolver=2000, maxitSIMPLE=MAX_OUTER, N1=2, N2=2, porevalue=0,
                                direction=1, border=0, method=method)
 
 
@@ -186,7 +188,7 @@ def run_reference(args):
     outer = 2
     rates = []
     for i in range(args.warmup + args.steps):
-        m = METHODS[i % 4]
+        m = METHODS[i % len(METHODS)]
         dt, rows, _ = cpu_sample(capi, img, m, outer)
         full = FULL_SOLVE_KRYLOV_ROWS.get(m)
         if i >= args.warmup:
@@ -223,7 +225,7 @@ def run_gpu(args):
     sizes = solvers["SIMPLEC"].sizes
 
     def step(i):
-        s = solvers[METHODS[i % 4]]
+        s = solvers[METHODS[i % len(METHODS)]]
         s.set_initial_fields()
         return s.solve()
 
@@ -256,25 +258,25 @@ def run_gpu(args):
     peak, peak_kind = load_peaks()
     achieved = SPMV_BYTES_PER_ROW * spmv_rows / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
     traffic = ncu_traffic()
-    kr_rows = {METHODS[i % 4]: int(results[i].krylov_rows) for i in range(len(results))}
-    outer_its = {METHODS[i % 4]: int(results[i].iterations) for i in range(len(results))}
-    ks = {METHODS[i % 4]: float(results[i].K) for i in range(len(results))}
+    kr_rows = {METHODS[i % len(METHODS)]: int(results[i].krylov_rows) for i in range(len(results))}
+    outer_its = {METHODS[i % len(METHODS)]: int(results[i].iterations) for i in range(len(results))}
+    ks = {METHODS[i % len(METHODS)]: float(results[i].K) for i in range(len(results))}
     cell_updates = sum(sizes.np * (r.iterations + 1) for r in results)
     # end to end through the C-ABI with host buffers
-    e2e_steps = min(args.steps, 4)
+    e2e_steps = 0 if args.no_e2e else min(args.steps, len(METHODS))
     h2d = raw.nbytes
     d2h = 8 * (sizes.np + sizes.nu + sizes.nv + sizes.nw)
     barrier(dist)
     t1 = time.perf_counter()
     for i in range(e2e_steps):
-        m = METHODS[i % 4]
+        m = METHODS[i % len(METHODS)]
         s = capi.Solver(lib, workload_params(capi, lib, m), raw, img.shape)
         s.solve()
         f = s.fields()
         s.close()
         assert f[0].size == sizes.np
     e2e_elapsed = reduce_max(dist, time.perf_counter() - t1)
-    e2e_value = world * e2e_steps / e2e_elapsed
+    e2e_value = world * e2e_steps / e2e_elapsed if e2e_steps else None
     line = None
     if rank == 0:
         cpu = None
@@ -327,7 +329,14 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
+    ap.add_argument("--max-outer", type=int, default=2000,
+                    help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
+    global METHODS, MAX_OUTER
+    METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]
+    MAX_OUTER = args.max_outer
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
