@@ -323,6 +323,7 @@ def run_gpu(args):
 
 
 def main():
+    global METHODS, MAX_OUTER
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -334,7 +335,6 @@ def main():
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
-    global METHODS, MAX_OUTER
     METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]
     MAX_OUTER = args.max_outer
     if args.impl == "reference":
