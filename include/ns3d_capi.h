@@ -240,6 +240,27 @@ typedef struct ns3d_profile {
 NS3D_API int ns3d_set_profiling(ns3d_handle *h, int32_t enable);
 NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
 
+/*
+ * BiCGSTAB that allocates nothing.  No counterpart in the reference: it
+ * exists for callers that cannot call cudaMalloc -- hosts running inside
+ * another framework's memory pool or reserving all device memory at start-up,
+ * and hosts that forbid allocation after initialisation.  The caller passes a
+ * system already in device memory (coef 7*npad doubles slot-major
+ * [P,W,E,S,N,B,T], nbr 6*npad int32 [W,E,S,N,B,T], -1 = no entry, npad a
+ * multiple of 1024 and >= n), the right-hand side and the guess/solution x
+ * (npad doubles each) and a CUDA stream (NULL = default stream).  Work vectors
+ * live in a fixed device array inside the library: at most 65536 rows
+ * (larger n returns NS3D_ERR_ARG); the array (about 4.6 MiB) is held on every
+ * GPU that loads the library until exit.  The first call on a device looks
+ * up the array's device address (cudaGetSymbolAddress), so make it before any
+ * stream capture.  All calls share the array: calls that overlap on the GPU
+ * race and must be serialized by the caller.  Same arithmetic and results as
+ * ns3d_solve_system.  Error text: ns3d_noalloc_last_error().
+ */
+NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t *nbr, const double *rhs, double *x, int32_t n,
+                                   int32_t npad, double tol, int32_t maxit, void *stream, ns3d_solve_info *info);
+NS3D_API const char *ns3d_noalloc_last_error(void);
+
 /* ---- host utilities (CUDA library only; no device work) ----------------- */
 /*
  * Parse an ini file like ReadInput (src/navierstokes3D.cxx:266-463): same
