@@ -51,6 +51,7 @@ SPMV_BYTES_PER_ROW = 104  # 7*8 coefficients + 6*4 indices + 8 gathered x + 8 do
 FULL_SOLVE_KRYLOV_ROWS = {"SIMPLEC": 246125574149, "SIMPLER": 316246186905, "SIMPLERR": 325991783660,
                           "IDEAL": 87945733905}
 MAX_OUTER = 2000
+PRECISION = 0  # 0 plain FP64, 1 mixed (FP32 inner / FP64 outer)
 
 
 def workload_params(capi, lib, method):
@@ -58,7 +59,7 @@ def workload_params(capi, lib, method):
     return capi.default_params(lib, dx=dx, dy=-1.0, dz=-1.0, mu=1e-3, rho=1.0, p0=1.0, gradp=1.0 / (SHAPE[0] * dx),
                                alpha=0.5, beta=1.0, vsolvertol=1e-8, psolvertol=1e-8, pcsolvertol=1e-8,
                                simpletol=1e-6, maxitsolver=2000, maxitSIMPLE=MAX_OUTER, N1=2, N2=2, porevalue=0,
-                               direction=1, border=0, method=method)
+                               direction=1, border=0, method=method, precision=PRECISION)
 
 
 def make_image():
@@ -323,7 +324,7 @@ def run_gpu(args):
 
 
 def main():
-    global METHODS, MAX_OUTER
+    global METHODS, MAX_OUTER, PRECISION
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -332,11 +333,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
     METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]
     MAX_OUTER = args.max_outer
+    PRECISION = 1 if args.precision == "mixed" else 0
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -14,14 +14,15 @@ namespace ns3d {
 
 // ---- fixed-order reductions ---------------------------------------------
 // Rows are cut into chunks of CH = 1024.  A chunk is processed by one block
-// of LANES = 256 threads; thread (lane) l owns rows 4l..4l+3 of the chunk and
-// accumulates them in order.  The 256 lane values are combined by a halving
-// tree (offsets 128, 64, ..., 1).  Chunk partials of one system are combined
-// the same way by the last block to finish: lane l sums partials l, l+256, ...
-// in order, then the tree.
-constexpr int CH = 1024;
-constexpr int LANES = 256;
-constexpr int RPL = 4;
+// of LANES = 128 threads; thread (lane) l owns rows l, l+128, ..., l+896 of
+// the chunk (coalesced) and accumulates them in that order.  Each warp's 32
+// lane values are combined by a halving tree (offsets 16, 8, 4, 2, 1), then
+// the 4 warp sums by a halving tree (offsets 2, 1).  Chunk partials of one
+// system are combined the same way by the last block to finish: lane l sums
+// partials l, l+128, ... in order, then the trees.
+constexpr int LANES = 128;
+constexpr int RPL = 8;
+constexpr int CH = LANES * RPL;
 
 __device__ __forceinline__ double warp_tree_sum(double v) {
     // offsets 16..1 of the halving tree inside one warp; lane 0 ends with the
@@ -38,16 +39,13 @@ __device__ __forceinline__ double warp_tree_sum(double v) {
 // threads get an unspecified value).  `sm` needs LANES doubles.
 __device__ __forceinline__ double block_tree_sum(double v, double *sm) {
     const int t = threadIdx.x;
-    sm[t] = v;
-    __syncthreads();
-    if (t < 128) sm[t] = sm[t] + sm[t + 128];
-    __syncthreads();
-    if (t < 64) sm[t] = sm[t] + sm[t + 64];
+    v = warp_tree_sum(v);
+    if ((t & 31) == 0) sm[t >> 5] = v;
     __syncthreads();
     double r = 0.0;
     if (t < 32) {
-        r = sm[t] + sm[t + 32];
-        r = warp_tree_sum(r);
+        r = (t < LANES / 32) ? sm[t] : 0.0;
+        for (int off = LANES / 64; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
     }
     __syncthreads();
     return r;
@@ -56,31 +54,23 @@ __device__ __forceinline__ double block_tree_sum(double v, double *sm) {
 __device__ __forceinline__ double dmaxv(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double dminv(double a, double b) { return (b < a) ? b : a; }
 
-// tree of maxima (order is irrelevant for max, kept identical for clarity)
-__device__ __forceinline__ double block_tree_max(double v, double *sm) {
+// maxima / minima over the block (exact in any order); result in every thread
+template <bool MAX>
+__device__ __forceinline__ double block_extreme(double v, double *sm) {
     const int t = threadIdx.x;
-    sm[t] = v;
-    __syncthreads();
-    for (int off = 128; off >= 1; off >>= 1) {
-        if (t < off) sm[t] = dmaxv(sm[t], sm[t + off]);
-        __syncthreads();
+    for (int off = 16; off >= 1; off >>= 1) {
+        double o = __shfl_down_sync(0xffffffffu, v, off);
+        v = MAX ? dmaxv(v, o) : dminv(v, o);
     }
+    if ((t & 31) == 0) sm[t >> 5] = v;
+    __syncthreads();
     double r = sm[0];
+    for (int w = 1; w < LANES / 32; ++w) r = MAX ? dmaxv(r, sm[w]) : dminv(r, sm[w]);
     __syncthreads();
     return r;
 }
-__device__ __forceinline__ double block_tree_min(double v, double *sm) {
-    const int t = threadIdx.x;
-    sm[t] = v;
-    __syncthreads();
-    for (int off = 128; off >= 1; off >>= 1) {
-        if (t < off) sm[t] = dminv(sm[t], sm[t + off]);
-        __syncthreads();
-    }
-    double r = sm[0];
-    __syncthreads();
-    return r;
-}
+__device__ __forceinline__ double block_tree_max(double v, double *sm) { return block_extreme<true>(v, sm); }
+__device__ __forceinline__ double block_tree_min(double v, double *sm) { return block_extreme<false>(v, sm); }
 
 // Final combination of `n` chunk partials (strided by `stride` doubles):
 // lane l sums partials l, l+256, ... in order, then the halving tree.

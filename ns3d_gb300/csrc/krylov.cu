@@ -31,53 +31,69 @@
 
 namespace ns3d {
 
-struct Row4 {
-    double v[4];
+struct Row4 {  // a thread's RPL rows
+    double v[RPL];
 };
 
+// A thread's rows are r0 + m*LANES, m < RPL (coalesced across the warp).
 __device__ __forceinline__ Row4 ld4(const double *p) {
-    const double2 a = *reinterpret_cast<const double2 *>(p);
-    const double2 b = *reinterpret_cast<const double2 *>(p + 2);
     Row4 r;
-    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
-    return r;
-}
-__device__ __forceinline__ Row4 ld4cg(const double *p) {
-    const double2 a = __ldcg(reinterpret_cast<const double2 *>(p));
-    const double2 b = __ldcg(reinterpret_cast<const double2 *>(p + 2));
-    Row4 r;
-    r.v[0] = a.x; r.v[1] = a.y; r.v[2] = b.x; r.v[3] = b.y;
+#pragma unroll
+    for (int m = 0; m < RPL; ++m) r.v[m] = p[m * LANES];
     return r;
 }
 __device__ __forceinline__ void st4(double *p, const Row4 &r) {
-    *reinterpret_cast<double2 *>(p) = make_double2(r.v[0], r.v[1]);
-    *reinterpret_cast<double2 *>(p + 2) = make_double2(r.v[2], r.v[3]);
+#pragma unroll
+    for (int m = 0; m < RPL; ++m) p[m * LANES] = r.v[m];
 }
-__device__ __forceinline__ int4 ldi4(const int *p) { return *reinterpret_cast<const int4 *>(p); }
 
-// y = A x for the 4 consecutive rows r0..r0+3 (rows >= n give garbage that
-// callers mask).  Each row: fma chain in ascending column order from 0.
-__device__ __forceinline__ Row4 spmv4(const KSys &S, int r0, const double *__restrict__ x) {
+// One row of y = A x: fma chain in ascending column order from 0 (the order
+// of row_ordered in device.cuh).  Every gather is issued unconditionally (a
+// missing neighbour reads the row's own element) so the loads of a row do
+// not wait on each other; only the fused multiply-adds are predicated.  The
+// two rare orders (W directly before the row, E directly after it) are taken
+// only by warps that contain such a row.
+__device__ __forceinline__ double spmv_row(const KSys &S, int row, const double *__restrict__ x) {
     const size_t np = (size_t)S.npad;
-    const int4 iW = ldi4(S.nbr + 0 * np + r0), iE = ldi4(S.nbr + 1 * np + r0);
-    const int4 iS = ldi4(S.nbr + 2 * np + r0), iN = ldi4(S.nbr + 3 * np + r0);
-    const int4 iB = ldi4(S.nbr + 4 * np + r0), iT = ldi4(S.nbr + 5 * np + r0);
-    const Row4 cP = ld4(S.coef + 0 * np + r0), cW = ld4(S.coef + 1 * np + r0), cE = ld4(S.coef + 2 * np + r0);
-    const Row4 cS = ld4(S.coef + 3 * np + r0), cN = ld4(S.coef + 4 * np + r0), cB = ld4(S.coef + 5 * np + r0);
-    const Row4 cT = ld4(S.coef + 6 * np + r0);
-    const int aW[4] = {iW.x, iW.y, iW.z, iW.w}, aE[4] = {iE.x, iE.y, iE.z, iE.w};
-    const int aS[4] = {iS.x, iS.y, iS.z, iS.w}, aN[4] = {iN.x, iN.y, iN.z, iN.w};
-    const int aB[4] = {iB.x, iB.y, iB.z, iB.w}, aT[4] = {iT.x, iT.y, iT.z, iT.w};
+    const int *nb = S.nbr + row;
+    const double *cf = S.coef + row;
+    const int nW = nb[0 * np], nE = nb[1 * np], nS = nb[2 * np], nN = nb[3 * np], nB = nb[4 * np],
+              nT = nb[5 * np];
+    const double xP = x[row];
+    const double xW = x[nW >= 0 ? nW : row], xE = x[nE >= 0 ? nE : row], xS = x[nS >= 0 ? nS : row];
+    const double xN = x[nN >= 0 ? nN : row], xB = x[nB >= 0 ? nB : row], xT = x[nT >= 0 ? nT : row];
+    const double cP = cf[0], cW = cf[1 * np], cE = cf[2 * np], cS = cf[3 * np], cN = cf[4 * np],
+                 cB = cf[5 * np], cT = cf[6 * np];
+    const bool wlate = nW >= 0 && nW == row - 1;
+    const bool eearly = nE >= 0 && nE == row + 1;
+    double acc = 0.0;
+    if (__any_sync(0xffffffffu, wlate || eearly)) {
+        if (!wlate && nW >= 0) acc = __fma_rn(cW, xW, acc);
+        if (nS >= 0) acc = __fma_rn(cS, xS, acc);
+        if (nB >= 0) acc = __fma_rn(cB, xB, acc);
+        if (wlate) acc = __fma_rn(cW, xW, acc);
+        acc = __fma_rn(cP, xP, acc);
+        if (eearly) acc = __fma_rn(cE, xE, acc);
+        if (nT >= 0) acc = __fma_rn(cT, xT, acc);
+        if (nN >= 0) acc = __fma_rn(cN, xN, acc);
+        if (!eearly && nE >= 0) acc = __fma_rn(cE, xE, acc);
+    } else {
+        if (nW >= 0) acc = __fma_rn(cW, xW, acc);
+        if (nS >= 0) acc = __fma_rn(cS, xS, acc);
+        if (nB >= 0) acc = __fma_rn(cB, xB, acc);
+        acc = __fma_rn(cP, xP, acc);
+        if (nT >= 0) acc = __fma_rn(cT, xT, acc);
+        if (nN >= 0) acc = __fma_rn(cN, xN, acc);
+        if (nE >= 0) acc = __fma_rn(cE, xE, acc);
+    }
+    return acc;
+}
+
+// y = A x for the thread's rows (rows >= n give garbage that callers mask)
+__device__ __forceinline__ Row4 spmv4(const KSys &S, int r0, const double *__restrict__ x) {
     Row4 out;
 #pragma unroll
-    for (int m = 0; m < 4; ++m) {
-        const int row = r0 + m;
-        out.v[m] = row_ordered(row, aW[m], aE[m], aS[m], aN[m], aB[m], aT[m], [&](double acc, int s, int col) {
-            const double c = s == SP ? cP.v[m] : s == SW ? cW.v[m] : s == SE ? cE.v[m] : s == SS ? cS.v[m]
-                           : s == SN ? cN.v[m] : s == SB ? cB.v[m] : cT.v[m];
-            return __fma_rn(c, x[col], acc);
-        });
-    }
+    for (int m = 0; m < RPL; ++m) out.v[m] = spmv_row(S, r0 + m * LANES, x);
     return out;
 }
 
@@ -100,7 +116,7 @@ __device__ __forceinline__ ChunkCtx chunk_ctx(const KSys *sys, const int *chunk_
     cx.active = sh[1] != 0;
     __syncthreads();
     cx.lc = c - sys[cx.sys].chunk_begin;
-    cx.r0 = cx.lc * CH + threadIdx.x * RPL;
+    cx.r0 = cx.lc * CH + threadIdx.x;
     return cx;
 }
 
@@ -138,9 +154,9 @@ __global__ void __launch_bounds__(LANES) k_kr_init(const KSys *__restrict__ sys,
             const Row4 b = ld4(S.b + cx.r0);
             Row4 r;
 #pragma unroll
-            for (int m = 0; m < 4; ++m) {
+            for (int m = 0; m < RPL; ++m) {
                 r.v[m] = b.v[m] - ax.v[m];
-                if (cx.r0 + m < S.n) {
+                if (cx.r0 + m * LANES < S.n) {
                     arr = __fma_rn(r.v[m], r.v[m], arr);
                     abb = __fma_rn(b.v[m], b.v[m], abb);
                 }
@@ -202,8 +218,10 @@ __global__ void k_kr_init2(const KSys *__restrict__ sys, const int *__restrict__
         __syncthreads();
         const KSys &S = sys[sh[0]];
         __syncthreads();
-        const int r0 = (c - S.chunk_begin) * CH + threadIdx.x * RPL;
-        const Row4 z = {{0.0, 0.0, 0.0, 0.0}};
+        const int r0 = (c - S.chunk_begin) * CH + threadIdx.x;
+        Row4 z;
+#pragma unroll
+        for (int m = 0; m < RPL; ++m) z.v[m] = 0.0;
         st4(S.p + r0, z);
         st4(S.v + r0, z);
         if (__ldcg(&S.st->zero_rhs)) st4(S.x + r0, z);
@@ -222,7 +240,7 @@ __global__ void __launch_bounds__(LANES) k_kr_p(const KSys *__restrict__ sys, co
         const Row4 r = ld4(S.r + cx.r0), v = ld4(S.v + cx.r0), iv = ld4(S.invdiag + cx.r0);
         Row4 p = ld4(S.p + cx.r0), y;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
+        for (int m = 0; m < RPL; ++m) {
             p.v[m] = __fma_rn(beta, __fma_rn(-w, v.v[m], p.v[m]), r.v[m]);
             y.v[m] = iv.v[m] * p.v[m];
         }
@@ -244,8 +262,8 @@ __global__ void __launch_bounds__(LANES) k_kr_v(const KSys *__restrict__ sys, co
         const Row4 r0 = ld4(S.r0 + cx.r0);
         double a = 0.0;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-            if (cx.r0 + m < S.n) a = __fma_rn(r0.v[m], v.v[m], a);
+        for (int m = 0; m < RPL; ++m)
+            if (cx.r0 + m * LANES < S.n) a = __fma_rn(r0.v[m], v.v[m], a);
         st4(S.v + cx.r0, v);
         double t = block_tree_sum(a, sm);
         if (threadIdx.x == 0) S.part[2 * (size_t)cx.lc] = t;
@@ -271,7 +289,7 @@ __global__ void __launch_bounds__(LANES) k_kr_s(const KSys *__restrict__ sys, co
         const Row4 r = ld4(S.r + cx.r0), v = ld4(S.v + cx.r0), iv = ld4(S.invdiag + cx.r0);
         Row4 s, z;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
+        for (int m = 0; m < RPL; ++m) {
             s.v[m] = __fma_rn(-alpha, v.v[m], r.v[m]);
             z.v[m] = iv.v[m] * s.v[m];
         }
@@ -293,8 +311,8 @@ __global__ void __launch_bounds__(LANES) k_kr_t(const KSys *__restrict__ sys, co
         const Row4 s = ld4(S.s + cx.r0);
         double att = 0.0, ats = 0.0;
 #pragma unroll
-        for (int m = 0; m < 4; ++m)
-            if (cx.r0 + m < S.n) {
+        for (int m = 0; m < RPL; ++m)
+            if (cx.r0 + m * LANES < S.n) {
                 att = __fma_rn(t.v[m], t.v[m], att);
                 ats = __fma_rn(t.v[m], s.v[m], ats);
             }
@@ -331,10 +349,10 @@ __global__ void __launch_bounds__(LANES) k_kr_x(const KSys *__restrict__ sys, co
         Row4 x = ld4(S.x + cx.r0), r;
         double a0r = 0.0, arr = 0.0;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
+        for (int m = 0; m < RPL; ++m) {
             x.v[m] = __fma_rn(w, z.v[m], __fma_rn(alpha, y.v[m], x.v[m]));
             r.v[m] = __fma_rn(-w, t.v[m], s.v[m]);
-            if (cx.r0 + m < S.n) {
+            if (cx.r0 + m * LANES < S.n) {
                 a0r = __fma_rn(r0.v[m], r.v[m], a0r);
                 arr = __fma_rn(r.v[m], r.v[m], arr);
             }
@@ -391,15 +409,15 @@ __global__ void __launch_bounds__(LANES) k_kr_restart(const KSys *__restrict__ s
         __syncthreads();
         if (!act) continue;
         const KSys &S = sys[sidx];
-        const int lc = c - S.chunk_begin, r0i = lc * CH + threadIdx.x * RPL;
+        const int lc = c - S.chunk_begin, r0i = lc * CH + threadIdx.x;
         const Row4 ax = spmv4(S, r0i, S.x);
         const Row4 b = ld4(S.b + r0i);
         Row4 r;
         double arr = 0.0;
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
+        for (int m = 0; m < RPL; ++m) {
             r.v[m] = b.v[m] - ax.v[m];
-            if (r0i + m < S.n) arr = __fma_rn(r.v[m], r.v[m], arr);
+            if (r0i + m * LANES < S.n) arr = __fma_rn(r.v[m], r.v[m], arr);
         }
         st4(S.r + r0i, r);
         st4(S.r0 + r0i, r);
@@ -425,7 +443,7 @@ __global__ void k_spmv(SysView A, const double *__restrict__ x, double *__restri
     KSys S;
     S.n = A.n; S.npad = A.npad; S.coef = A.coef; S.nbr = A.nbr;
     for (int c = blockIdx.x; c < A.nchunks; c += gridDim.x) {
-        const int r0 = c * CH + threadIdx.x * RPL;
+        const int r0 = c * CH + threadIdx.x;
         const Row4 v = spmv4(S, r0, x);
         st4(y + r0, v);
     }
@@ -446,7 +464,9 @@ int device_sm_count() {
     return g_sms;
 }
 
-static inline int kr_grid(int total_chunks) { return std::max(1, std::min(total_chunks, device_sm_count() * 6)); }
+// one block per chunk up to 32 blocks per SM (the hardware schedules the
+// waves); beyond that, blocks walk the chunks grid-stride
+static inline int kr_grid(int total_chunks) { return std::max(1, std::min(total_chunks, device_sm_count() * 32)); }
 
 void launch_krylov_init(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
     (void)nsys;

@@ -1,0 +1,36 @@
+// mixed.h -- data of the mixed-precision (FP32 inner / FP64 outer) solves.
+#pragma once
+
+#include "device.cuh"
+
+namespace ns3d {
+
+// FP64 defect-correction state of one system
+struct DCState {
+    double rr, bb, tol, tol2, scale, error, tin, tin_min;
+    int total_iter, maxit, done, info, zero_rhs, pad_;
+    unsigned int counter, pad2_;
+};
+
+struct MSys {
+    int n, npad, nchunks, chunk_begin;
+    const int *nbr;
+    const double *coef64;  // [7][npad]
+    const double *b64;     // right-hand side
+    double *x64;           // guess in, solution out
+    double *r64;           // FP64 residual
+    const float *coef32, *invdiag32;
+    float *x, *r, *r0, *p, *v, *y, *s, *z, *t;  // FP32 inner vectors (x is the correction)
+    double *part;
+    KState *st;  // inner BiCGSTAB state (scalars in FP64)
+    DCState *dc;
+};
+
+void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
+                   cudaStream_t st);
+void launch_dc_resid(const MSys *sys, const int *chunk_sys, int total_chunks, int first, cudaStream_t st);
+void launch_m32_init(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
+void launch_m32_iteration(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
+void launch_dc_update(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
+
+}  // namespace ns3d

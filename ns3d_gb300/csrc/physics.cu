@@ -661,7 +661,7 @@ __global__ void k_permeability(Grid g, const double *__restrict__ u, const doubl
     for (int c = blockIdx.x; c < nch; c += gridDim.x) {
         double a = 0, so = 0, si = 0, co = 0, ci = 0;
         for (int m = 0; m < RPL; ++m) {
-            long q = (long)c * CH + threadIdx.x * RPL + m;
+            long q = (long)c * CH + threadIdx.x + LANES * m;
             if (q >= plane) break;
             int r = g.umap[(long)iu * plane + q];
             if (r > -1) a = a + u[r];
@@ -712,7 +712,7 @@ __global__ void k_divergence(Grid g, Phys ph, SysView P, const double *__restric
     for (int c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
         double s2 = 0, sv = 0, mdv = 0, mdiv = 0;
         for (int m = 0; m < RPL; ++m) {
-            int r = c * CH + threadIdx.x * RPL + m;
+            int r = c * CH + threadIdx.x + LANES * m;
             if (r >= P.n) break;
             int i, j, k, f;
             g.ijk(P.cell[r], i, j, k);
@@ -787,7 +787,7 @@ __global__ void k_correct_pressure(SysView P, const double *__restrict__ pc, dou
     for (int c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
         double mx = -HUGE_VAL, mn = HUGE_VAL, sq = 0;
         for (int m = 0; m < RPL; ++m) {
-            int r = c * CH + threadIdx.x * RPL + m;
+            int r = c * CH + threadIdx.x + LANES * m;
             if (r >= P.n) break;
             double x = pc[r];
             mx = (x > mx) ? x : mx;

@@ -7,6 +7,7 @@
 #include <string>
 #include <vector>
 
+#include "../../include/ns3d_capi.h"
 #include "device.cuh"
 #include "kernels.h"
 
@@ -86,7 +87,11 @@ struct DevSys {
     DBuf<int> nbr;
     DBuf<double> rhs, rowsum, invdiag;
     DBuf<double> r, r0, p, v, y, s, z, t, part;
+    // FP32 copy of the system and the FP32 Krylov vectors (mixed precision),
+    // allocated on first use
+    DBuf<float> coef32, invdiag32, fx, fr, fr0, fp, fv, fy, fs, fz, ft;
     void allocate(int rows, int first_extent, cudaStream_t st);
+    void allocate_f32(cudaStream_t st);
     SysView view() const {
         SysView sv;
         sv.n = n;
@@ -149,6 +154,35 @@ class KrylovSet {
     int nsys_ = 0, total_chunks_ = 0;
     int prev_iters_ = 8;
     long launches_ = 0;
+};
+
+struct MSys;
+struct DCState;
+
+// A set of systems solved by FP32 BiCGSTAB inside FP64 defect correction.
+// The FP32 copy of each matrix is refreshed from the FP64 one at every run.
+class MixedSet {
+  public:
+    void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out);
+    const KState *inner_state(int i) const { return st_.p + i; }
+    // FP64 outcome of system i, mirrored into a KState (iter, info) for the
+    // velocity post-processing kernel
+    const KState *device_state(int i) const { return out_st_.p + i; }
+    double inner_rel_tol = 1e-4;  // floor of the per-round FP32 reduction target
+    ~MixedSet() = default;
+
+  private:
+    void configure(const std::vector<SolveItem> &items, cudaStream_t st);
+    DBuf<MSys> msys_;
+    DBuf<int> chunk_sys_;
+    DBuf<KState> st_, out_st_;
+    DBuf<DCState> dc_;
+    HBuf<KState> h_st_, h_out_;
+    HBuf<DCState> h_dc_;
+    HBuf<MSys> h_msys_;
+    std::vector<const double *> key_;
+    int nsys_ = 0, total_chunks_ = 0;
+    int prev_iters_ = 8;
 };
 
 }  // namespace ns3d

@@ -231,6 +231,12 @@ struct ns3d_handle {
     DBuf<DiagOut> diag;
     HBuf<DiagOut> h_diag;
     KrylovSet kmom, kp;
+    MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
+    bool mixed() const { return prm.precision == NS3D_MIXED; }
+    void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
+        if (mixed()) mp.run(items, stream, out);
+        else kp.run(items, stream, out);
+    }
 
     // physical constants and relaxation state (NavierStokesBase members)
     double dx, dy, dz, mu, rho, p0, p1, gradp, alpha0, beta0, alpha, beta;
@@ -399,10 +405,12 @@ void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
                                     {&V, v.p, V.rhs.p, prm.vsolvertol, prm.maxitsolver}};
     if (nw > 0) items.push_back({&W, w.p, W.rhs.p, prm.vsolvertol, prm.maxitsolver});
     std::vector<SolveOutcome> out;
-    kmom.run(items, stream, out);
-    launch_velocity_post(utemp.p, u.p, nu, kmom.device_state(0), limit, dvmax, stream);
-    launch_velocity_post(vtemp.p, v.p, nv, kmom.device_state(1), limit, dvmax, stream);
-    if (nw > 0) launch_velocity_post(wtemp.p, w.p, nw, kmom.device_state(2), limit, dvmax, stream);
+    if (mixed()) mmom.run(items, stream, out);
+    else kmom.run(items, stream, out);
+    auto state = [&](int i) { return mixed() ? mmom.device_state(i) : kmom.device_state(i); };
+    launch_velocity_post(utemp.p, u.p, nu, state(0), limit, dvmax, stream);
+    launch_velocity_post(vtemp.p, v.p, nv, state(1), limit, dvmax, stream);
+    if (nw > 0) launch_velocity_post(wtemp.p, w.p, nw, state(2), limit, dvmax, stream);
     su = out[0];
     sv = out[1];
     if (nw > 0) sw = out[2];
@@ -431,7 +439,7 @@ void ns3d_handle::log_pressure_status(const SolveOutcome &o) {
 void ns3d_handle::compute_pressure_correction() {
     info.s("Solving for pressure correction : ");
     std::vector<SolveOutcome> out;
-    kp.run({{&P, pc.p, P.rhs.p, prm.pcsolvertol, prm.maxitsolver}}, stream, out);
+    solve_p({{&P, pc.p, P.rhs.p, prm.pcsolvertol, prm.maxitsolver}}, out);
     sp = out[0];
     res.krylov_iterations += sp.work;
     res.krylov_rows += (int64_t)sp.work * np;
@@ -444,13 +452,13 @@ void ns3d_handle::compute_pressure_field() {
     info.s("Solving for pressure in : ");
     d2d(ptemp.p, p.p, P.npad);
     std::vector<SolveOutcome> out;
-    kp.run({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, stream, out);
+    solve_p({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, out);
     sp = out[0];
     res.krylov_iterations += sp.work;
     res.krylov_rows += (int64_t)sp.work * np;
     while (sp.iters == 0 && sp.info == NS3D_SUCCESS && tol > 1e-15) {
         tol *= 0.1;
-        kp.run({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, stream, out);
+        solve_p({{&P, ptemp.p, P.rhs.p, tol, prm.maxitsolver}}, out);
         sp = out[0];
         res.krylov_iterations += sp.work;
         res.krylov_rows += (int64_t)sp.work * np;
@@ -996,7 +1004,6 @@ NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, 
 NS3D_API int ns3d_solve(ns3d_handle *H) {
     NS3D_TRY
     ns3d_handle &h = *checked(H);
-    if (h.prm.precision != NS3D_FP64) throw ApiError(NS3D_ERR_UNSUPPORTED, "mixed precision is not built yet");
     std::memset(&h.res, 0, sizeof h.res);
     h.su = h.sv = h.sw = h.sp = SolveOutcome();
     h.alpha = h.alpha0;
@@ -1091,9 +1098,14 @@ NS3D_API int ns3d_solve_system(ns3d_handle *H, int32_t sys, const double *rhs, d
         NS3D_CUDA_CHECK(cudaMemcpyAsync(db.p, rhs, (size_t)S.n * 8, cudaMemcpyHostToDevice, h.stream));
         b = db.p;
     }
-    KrylovSet ks;
     std::vector<SolveOutcome> out;
-    ks.run({{&S, dx.p, b, tol, maxit}}, h.stream, out);
+    if (h.mixed()) {
+        MixedSet ms;
+        ms.run({{&S, dx.p, b, tol, maxit}}, h.stream, out);
+    } else {
+        KrylovSet ks;
+        ks.run({{&S, dx.p, b, tol, maxit}}, h.stream, out);
+    }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(x, dx.p, (size_t)S.n * 8, cudaMemcpyDeviceToHost, h.stream));
     h.sync();
     if (info) {

@@ -30,10 +30,11 @@
  * Summation order.  Eigen's SIMD reduction order cannot be reproduced, so
  * every floating-point sum over rows here uses one fixed, documented order
  * (det_sum below) that the CUDA kernels reproduce exactly: rows are cut into
- * chunks of 1024; inside a chunk, lane l (0..255) accumulates rows
- * 4l..4l+3 in order; the 256 lane values are combined by a halving tree
- * (offsets 128,64,...,1); chunk partials are combined the same way (lane l
- * sums partials l, l+256, ... in order, then the tree).  Sparse rows are
+ * chunks of 1024; inside a chunk, lane l (0..127) accumulates rows
+ * l, l+128, ..., l+896 in order; the lanes of each group of 32 are combined
+ * by a halving tree (offsets 16,8,4,2,1), then the 4 group sums by a halving
+ * tree (offsets 2,1); chunk partials are combined the same way (lane l
+ * sums partials l, l+128, ... in order, then the trees).  Sparse rows are
  * summed in ascending column order (Eigen's compressed row-major storage).
  * Fused multiply-adds appear only where written as std::fma; the file is
  * built with -ffp-contract=off so every other expression rounds as written.
@@ -73,13 +74,20 @@ int fail(int code, const char *fmt, ...) {
 
 /* ---------------- fixed-order reductions -------------------------------- */
 constexpr long CH = 1024;   // rows per chunk
-constexpr int LANES = 256;  // lanes per chunk
-constexpr int RPL = 4;      // consecutive rows per lane
+constexpr int LANES = 128;  // lanes per chunk
+constexpr int RPL = 8;      // rows per lane, strided by LANES
 
 inline double tree_sum(double *a) {
-    for (int off = LANES / 2; off >= 1; off >>= 1)
-        for (int l = 0; l < off; ++l) a[l] = a[l] + a[l + off];
-    return a[0];
+    double w[LANES / 32];
+    for (int g = 0; g < LANES / 32; ++g) {
+        double *b = a + 32 * g;
+        for (int off = 16; off >= 1; off >>= 1)
+            for (int l = 0; l < off; ++l) b[l] = b[l] + b[l + off];
+        w[g] = b[0];
+    }
+    for (int off = LANES / 64; off >= 1; off >>= 1)
+        for (int l = 0; l < off; ++l) w[l] = w[l] + w[l + off];
+    return w[0];
 }
 
 inline double final_sum(const std::vector<double> &part) {
@@ -103,7 +111,7 @@ double det_sum(long n, F f) {
         for (int l = 0; l < LANES; ++l) {
             double a = 0.0;
             for (int m = 0; m < RPL; ++m) {
-                long r = c * CH + (long)l * RPL + m;
+                long r = c * CH + (long)l + (long)LANES * m;
                 if (r < n) a = f(r, a);
             }
             acc[l] = a;
