@@ -261,6 +261,44 @@ NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t *nbr, const
                                    int32_t npad, double tol, int32_t maxit, void *stream, ns3d_solve_info *info);
 NS3D_API const char *ns3d_noalloc_last_error(void);
 
+/* ---- many solves on one GPU (no counterpart in the reference, which runs
+ * one image per process, src/navierstokes3D.cxx:516-542) ------------------- */
+/*
+ * Batch: solve njobs independent images concurrently, at most max_concurrent
+ * at a time, each on its own solver instance and CUDA stream.  raws[i] is the
+ * i-th raw image (VTK order), dims[3i..3i+2] its size.  results[i] and
+ * status[i] (may be NULL) receive each outcome.  Returns the worst status.
+ */
+NS3D_API int ns3d_batch_solve(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                              int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status);
+
+/*
+ * Server with continuous batching: requests are queued by ns3d_server_submit
+ * (the image is copied), admitted as soon as fewer than max_active solves run
+ * and the device has room for the request's estimated footprint
+ * (hbm_budget_bytes = 0: the free memory the device reports), solved on their
+ * own stream with their state resident in HBM until convergence, and
+ * retired; the next requests are admitted as memory frees up.
+ */
+typedef struct ns3d_server ns3d_server;
+typedef struct ns3d_server_stats {
+    int64_t completed, failed, queued;
+    int32_t active, peak_active;
+    double p50_latency_s, p99_latency_s, mean_latency_s;
+    double solves_per_s;  /* completed / (last completion - first submission) */
+} ns3d_server_stats;
+NS3D_API int ns3d_server_start(int32_t max_active, size_t hbm_budget_bytes, ns3d_server **out);
+/* keep_fields != 0 keeps the compacted fields for ns3d_server_fields */
+NS3D_API int ns3d_server_submit(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx, int32_t ny,
+                                int32_t nz, int32_t keep_fields, int64_t *ticket);
+/* state: 0 queued, 1 running, 2 done, 3 failed (the return value is the failure status) */
+NS3D_API int ns3d_server_poll(ns3d_server *s, int64_t ticket, int32_t *state, ns3d_result *result);
+NS3D_API int ns3d_server_wait(ns3d_server *s, int64_t ticket, ns3d_result *result, double *latency_s);
+NS3D_API int ns3d_server_fields(ns3d_server *s, int64_t ticket, double *p, double *u, double *v, double *w);
+NS3D_API int ns3d_server_get_stats(ns3d_server *s, ns3d_server_stats *out);
+/* finishes the queued and running requests, then frees the server */
+NS3D_API int ns3d_server_stop(ns3d_server *s);
+
 /* ---- host utilities (CUDA library only; no device work) ----------------- */
 /*
  * Parse an ini file like ReadInput (src/navierstokes3D.cxx:266-463): same

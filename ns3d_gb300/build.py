@@ -21,7 +21,7 @@ EXE = os.path.join(LIBDIR, "NS3D")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FILES = ["geometry.cu", "physics.cu", "krylov.cu", "solver.cu", "noalloc.cu", "mixed.cu", "mixed_host.cu"]
-CPP_FILES = ["hostio.cpp", "capi_host.cpp"]
+CPP_FILES = ["hostio.cpp", "capi_host.cpp", "serving.cpp"]
 
 
 def _nvcc():
@@ -68,8 +68,9 @@ def build(verbose=False, ptxas_info=False):
         obj = os.path.join(BUILD, f + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall",
-                         "-c", src, "-o", obj])
+            cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall", "-pthread",
+                         "-I" + cuda_inc, "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))
     if verbose:
@@ -77,7 +78,7 @@ def build(verbose=False, ptxas_info=False):
             if o.strip():
                 print(o)
     if _stale(LIB, objs):
-        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lz", "-Xlinker", "-Bsymbolic"])
+        _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs + ["-lz", "-lpthread", "-Xlinker", "-Bsymbolic"])
     main_src = os.path.join(CSRC, "main.cpp")
     if _stale(EXE, [main_src, LIB]):
         _run(["g++", "-O2", "-std=c++17", main_src, "-o", EXE, "-L" + LIBDIR, "-lns3d_gb300",

@@ -242,3 +242,95 @@ class Solver:
             self.close()
         except Exception:
             pass
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("active", C.c_int32), ("peak_active", C.c_int32),
+                ("p50_latency_s", C.c_double), ("p99_latency_s", C.c_double), ("mean_latency_s", C.c_double),
+                ("solves_per_s", C.c_double)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
+def _declare_server(lib):
+    if getattr(lib, "_ns3d_server_declared", False):
+        return lib
+    sig = {
+        "ns3d_server_start": (C.c_int, [C.c_int32, C.c_size_t, _P(C.c_void_p)]),
+        "ns3d_server_submit": (C.c_int, [C.c_void_p, _P(Params), _P(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_int32, _P(C.c_int64)]),
+        "ns3d_server_poll": (C.c_int, [C.c_void_p, C.c_int64, _P(C.c_int32), _P(Result)]),
+        "ns3d_server_wait": (C.c_int, [C.c_void_p, C.c_int64, _P(Result), _P(C.c_double)]),
+        "ns3d_server_fields": (C.c_int, [C.c_void_p, C.c_int64, _d, _d, _d, _d]),
+        "ns3d_server_get_stats": (C.c_int, [C.c_void_p, _P(ServerStats)]),
+        "ns3d_server_stop": (C.c_int, [C.c_void_p]),
+        "ns3d_batch_solve": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32, _P(Result),
+                                       _i32]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    lib._ns3d_server_declared = True
+    return lib
+
+
+class Server:
+    """Continuous-batching solve server (ns3d_server_*)."""
+
+    def __init__(self, lib, max_active, hbm_budget_bytes=0):
+        self.lib = _declare_server(lib)
+        h = C.c_void_p()
+        rc = self.lib.ns3d_server_start(int(max_active), int(hbm_budget_bytes), C.byref(h))
+        if rc != 0:
+            raise NS3DError(rc, "server start failed")
+        self.h = h
+        self.sizes = {}
+
+    def submit(self, params, raw_xfastest, dims, keep_fields=False):
+        raw = np.ascontiguousarray(raw_xfastest, dtype=np.uint8).reshape(-1)
+        t = C.c_int64()
+        rc = self.lib.ns3d_server_submit(self.h, C.byref(params), _ptr(raw, C.c_uint8), int(dims[0]), int(dims[1]),
+                                         int(dims[2]), int(bool(keep_fields)), C.byref(t))
+        if rc != 0:
+            raise NS3DError(rc, "submit failed")
+        return t.value
+
+    def wait(self, ticket):
+        r = Result()
+        lat = C.c_double()
+        rc = self.lib.ns3d_server_wait(self.h, int(ticket), C.byref(r), C.byref(lat))
+        if rc != 0:
+            raise NS3DError(rc, "request %d failed: %s" % (ticket, self.lib.ns3d_last_error().decode()))
+        return r, lat.value
+
+    def poll(self, ticket):
+        st = C.c_int32()
+        r = Result()
+        rc = self.lib.ns3d_server_poll(self.h, int(ticket), C.byref(st), C.byref(r))
+        return st.value, r, rc
+
+    def fields(self, ticket, sizes):
+        out = [np.empty(n, np.float64) for n in sizes]
+        rc = self.lib.ns3d_server_fields(self.h, int(ticket), *[_ptr(x, C.c_double) for x in out])
+        if rc != 0:
+            raise NS3DError(rc, "fields of request %d unavailable" % ticket)
+        return out
+
+    def stats(self):
+        s = ServerStats()
+        self.lib.ns3d_server_get_stats(self.h, C.byref(s))
+        return s
+
+    def stop(self):
+        if getattr(self, "h", None):
+            self.lib.ns3d_server_stop(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.stop()
+        except Exception:
+            pass

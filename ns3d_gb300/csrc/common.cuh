@@ -51,6 +51,36 @@ __device__ __forceinline__ double block_tree_sum(double v, double *sm) {
     return r;
 }
 
+// Two tree sums at once, each with exactly the pairings of block_tree_sum.
+// After the first level of a warp, lanes 0-15 carry the first sum and lanes
+// 16-31 the second, so every later level is one shuffle and one add for
+// both (FP64 issue is scarce on this GPU).  Results valid in thread 0.
+__device__ __forceinline__ void block_tree_sum2(double a, double b, double *sm, double &ra, double &rb) {
+    static_assert(2 * (LANES / 32) <= 32, "warp sums of both trees fit one warp");
+    const int t = threadIdx.x;
+    ra = 0.0;
+    rb = 0.0;
+    const bool lo = (t & 16) == 0;
+    // offset 16: lane l < 16 forms a_l + a_(l+16), lane l >= 16 forms b_(l-16) + b_l
+    double v = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
+    v = v + __shfl_down_sync(0xffffffffu, v, 8);
+    v = v + __shfl_down_sync(0xffffffffu, v, 4);
+    v = v + __shfl_down_sync(0xffffffffu, v, 2);
+    v = v + __shfl_down_sync(0xffffffffu, v, 1);
+    constexpr int NW = LANES / 32;
+    if ((t & 31) == 0) sm[t >> 5] = v;
+    if ((t & 31) == 16) sm[NW + (t >> 5)] = v;
+    __syncthreads();
+    if (t < 32) {
+        double r = (t < 2 * NW) ? sm[t] : 0.0;
+        for (int off = NW / 2; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
+        const double r2 = __shfl_sync(0xffffffffu, r, NW);
+        ra = r;
+        rb = r2;
+    }
+    __syncthreads();
+}
+
 __device__ __forceinline__ double dmaxv(double a, double b) { return (b > a) ? b : a; }
 __device__ __forceinline__ double dminv(double a, double b) { return (b < a) ? b : a; }
 
@@ -73,12 +103,23 @@ __device__ __forceinline__ double block_tree_max(double v, double *sm) { return 
 __device__ __forceinline__ double block_tree_min(double v, double *sm) { return block_extreme<false>(v, sm); }
 
 // Final combination of `n` chunk partials (strided by `stride` doubles):
-// lane l sums partials l, l+256, ... in order, then the halving tree.
+// lane l sums partials l, l+LANES, ... in order, then the halving tree.
 // Result valid in thread 0.
 __device__ __forceinline__ double final_partials_sum(const double *part, int n, int stride, double *sm) {
     double a = 0.0;
     for (int i = threadIdx.x; i < n; i += LANES) a = a + __ldcg(part + (size_t)i * stride);
     return block_tree_sum(a, sm);
+}
+
+// final_partials_sum of the interleaved pairs part[2i] and part[2i+1]
+__device__ __forceinline__ void final_partials_sum2(const double *part, int n, double *sm, double &ra, double &rb) {
+    double a = 0.0, b = 0.0;
+    for (int i = threadIdx.x; i < n; i += LANES) {
+        const double2 q = __ldcg(reinterpret_cast<const double2 *>(part) + i);
+        a = a + q.x;
+        b = b + q.y;
+    }
+    block_tree_sum2(a, b, sm, ra, rb);
 }
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }

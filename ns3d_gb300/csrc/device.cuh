@@ -117,4 +117,12 @@ struct KSys {  // one system of a solve set (device array)
     KState *st;
 };
 
+// A solve set as a kernel argument (passed by value, read from constant
+// memory): the systems in chunk order, sys[0].chunk_begin == 0.
+constexpr int KMAX = 4;
+struct KSetArg {
+    int nsys, total_chunks;
+    KSys sys[KMAX];
+};
+
 }  // namespace ns3d

@@ -10,6 +10,7 @@ namespace ns3d {
 struct Grid;
 struct SysView;
 struct KSys;
+struct KSetArg;
 struct KState;
 
 // geometry.cu
@@ -71,14 +72,13 @@ void launch_face_average(const Grid &g, const double *u, const double *v, const 
                          cudaStream_t st);
 
 // krylov.cu: batched BiCGSTAB over a set of systems
-void launch_krylov_init(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st);
-void launch_krylov_iteration(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st);
-void launch_krylov_restart(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st);
+void launch_krylov_init(const KSetArg &set, cudaStream_t st);
+void launch_krylov_iteration(const KSetArg &set, cudaStream_t st);
+void launch_krylov_restart(const KSetArg &set, cudaStream_t st);
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st);
 int device_sm_count();
 // K1..K5 of one BiCGSTAB iteration launched one at a time (profiling)
-void launch_krylov_kernel(int which, const KSys *sys, int nsys, const int *chunk_sys, int total_chunks,
-                          cudaStream_t st);
+void launch_krylov_kernel(int which, const KSetArg &set, cudaStream_t st);
 // kernels launched by this library since it was loaded
 int64_t launch_count();
 void count_launches(int64_t n);

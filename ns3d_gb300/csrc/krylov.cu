@@ -10,10 +10,12 @@
 // |rho| < eps^2 |r0|^2 (the counter restarts on the first restart), and the
 // zero right-hand side rule (x = 0, Success, iterations() = max).
 //
-// A solve set holds several independent systems (the three momentum
-// components, or the pressure system, or many images).  Their rows are
-// processed as one list of 1024-row chunks; every kernel below walks the
-// chunks grid-stride, skips systems that have finished, and the block that
+// A solve set holds up to KMAX independent systems (the three momentum
+// components, or the pressure system).  Their rows are processed as one list
+// of 1024-row chunks; the set is passed to every kernel by value
+// (__grid_constant__), so a block finds its system and the system's arrays
+// in constant memory and only reads the system's done flag from global
+// memory.  Finished systems make their chunks return at once; the block that
 // completes the last chunk of a system reduces that system's partials and
 // updates its scalars on the device.  One BiCGSTAB iteration is five kernels:
 //   K1 p = r + beta (p - w v); y = D^-1 p
@@ -97,27 +99,19 @@ __device__ __forceinline__ Row4 spmv4(const KSys &S, int r0, const double *__res
     return out;
 }
 
-struct ChunkCtx {
-    int sys, lc, r0;  // system, local chunk, first row of this thread
-    bool active;
-};
+// system owning global chunk c (chunk_begin ascending, first system begins at 0)
+__device__ __forceinline__ int sys_of_chunk(const KSetArg &A, int c) {
+    int s = 0;
+#pragma unroll
+    for (int q = 1; q < KMAX; ++q)
+        if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
+    return s;
+}
 
-__device__ __forceinline__ ChunkCtx chunk_ctx(const KSys *sys, const int *chunk_sys, int c, int *sh) {
-    ChunkCtx cx;
-    if (threadIdx.x == 0) {
-        int s = chunk_sys[c];
-        const KState *st = sys[s].st;
-        int act = (__ldcg(&st->done) == 0 && __ldcg(&st->paused) == 0) ? 1 : 0;
-        sh[0] = s;
-        sh[1] = act;
-    }
-    __syncthreads();
-    cx.sys = sh[0];
-    cx.active = sh[1] != 0;
-    __syncthreads();
-    cx.lc = c - sys[cx.sys].chunk_begin;
-    cx.r0 = cx.lc * CH + threadIdx.x;
-    return cx;
+// the done/paused flags change only between kernels (or after the last
+// chunk of the system arrived), so every thread of a block reads the same
+__device__ __forceinline__ bool sys_active(const KSys &S) {
+    return (__ldcg(&S.st->done) | __ldcg(&S.st->paused)) == 0;
 }
 
 __device__ __forceinline__ bool arrive_last(KState *st, unsigned int total, int *sh) {
@@ -125,10 +119,10 @@ __device__ __forceinline__ bool arrive_last(KState *st, unsigned int total, int 
     if (threadIdx.x == 0) {
         __threadfence();
         unsigned int prev = atomicAdd(&st->counter, 1u);
-        sh[2] = (prev == total - 1) ? 1 : 0;
+        sh[0] = (prev == total - 1) ? 1 : 0;
     }
     __syncthreads();
-    bool last = sh[2] != 0;
+    bool last = sh[0] != 0;
     if (last) __threadfence();
     return last;
 }
@@ -140,39 +134,43 @@ __device__ __forceinline__ void finish_loop(KState *st) {
     st->info = (st->error <= st->tol) ? 0 : 2;
 }
 
+#define NS3D_CHUNK_LOOP                                                        \
+    for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {            \
+        const int sidx = sys_of_chunk(A, c);                                   \
+        const KSys &S = A.sys[sidx];                                           \
+        const int lc = c - S.chunk_begin;                                      \
+        const int r0 = lc * CH + threadIdx.x;
+
 // ---- init: r = b - A x, r0 = r, |r|^2, |b|^2 ---------------------------------
-__global__ void __launch_bounds__(LANES) k_kr_init(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                   int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_kr_init(const __grid_constant__ KSetArg A) {
     __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        const KSys &S = sys[cx.sys];
+    __shared__ int sh[2];
+    NS3D_CHUNK_LOOP
         double arr = 0.0, abb = 0.0;
         {
-            const Row4 ax = spmv4(S, cx.r0, S.x);
-            const Row4 b = ld4(S.b + cx.r0);
+            const Row4 ax = spmv4(S, r0, S.x);
+            const Row4 b = ld4(S.b + r0);
             Row4 r;
 #pragma unroll
             for (int m = 0; m < RPL; ++m) {
                 r.v[m] = b.v[m] - ax.v[m];
-                if (cx.r0 + m * LANES < S.n) {
+                if (r0 + m * LANES < S.n) {
                     arr = __fma_rn(r.v[m], r.v[m], arr);
                     abb = __fma_rn(b.v[m], b.v[m], abb);
                 }
             }
-            st4(S.r + cx.r0, r);
-            st4(S.r0 + cx.r0, r);
+            st4(S.r + r0, r);
+            st4(S.r0 + r0, r);
         }
-        double trr = block_tree_sum(arr, sm);
-        double tbb = block_tree_sum(abb, sm);
+        double trr, tbb;
+        block_tree_sum2(arr, abb, sm, trr, tbb);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = trr;
-            S.part[2 * (size_t)cx.lc + 1] = tbb;
+            S.part[2 * (size_t)lc + 0] = trr;
+            S.part[2 * (size_t)lc + 1] = tbb;
         }
         if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            double rr = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            double bb = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double rr, bb;
+            final_partials_sum2(S.part, S.nchunks, sm, rr, bb);
             if (threadIdx.x == 0) {
                 KState *st = S.st;
                 st->counter = 0;
@@ -211,14 +209,8 @@ __global__ void __launch_bounds__(LANES) k_kr_init(const KSys *__restrict__ sys,
 }
 
 // p = v = 0; x = 0 for a zero right-hand side
-__global__ void k_kr_init2(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys, int total_chunks) {
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        if (threadIdx.x == 0) sh[0] = chunk_sys[c];
-        __syncthreads();
-        const KSys &S = sys[sh[0]];
-        __syncthreads();
-        const int r0 = (c - S.chunk_begin) * CH + threadIdx.x;
+__global__ void k_kr_init2(const __grid_constant__ KSetArg A) {
+    NS3D_CHUNK_LOOP
         Row4 z;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) z.v[m] = 0.0;
@@ -229,46 +221,39 @@ __global__ void k_kr_init2(const KSys *__restrict__ sys, const int *__restrict__
 }
 
 // K1: p = r + beta (p - w v); y = D^-1 p
-__global__ void __launch_bounds__(LANES) k_kr_p(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                int total_chunks) {
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        if (!cx.active) continue;
-        const KSys &S = sys[cx.sys];
+__global__ void __launch_bounds__(LANES) k_kr_p(const __grid_constant__ KSetArg A) {
+    NS3D_CHUNK_LOOP
+        if (!sys_active(S)) continue;
         const double beta = __ldcg(&S.st->beta), w = __ldcg(&S.st->w);
-        const Row4 r = ld4(S.r + cx.r0), v = ld4(S.v + cx.r0), iv = ld4(S.invdiag + cx.r0);
-        Row4 p = ld4(S.p + cx.r0), y;
+        const Row4 r = ld4(S.r + r0), v = ld4(S.v + r0), iv = ld4(S.invdiag + r0);
+        Row4 p = ld4(S.p + r0), y;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             p.v[m] = __fma_rn(beta, __fma_rn(-w, v.v[m], p.v[m]), r.v[m]);
             y.v[m] = iv.v[m] * p.v[m];
         }
-        st4(S.p + cx.r0, p);
-        st4(S.y + cx.r0, y);
+        st4(S.p + r0, p);
+        st4(S.y + r0, y);
     }
 }
 
 // K2: v = A y, <r0, v> -> alpha = rho / <r0, v>
-__global__ void __launch_bounds__(LANES) k_kr_v(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_kr_v(const __grid_constant__ KSetArg A) {
     __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        if (!cx.active) continue;
-        const KSys &S = sys[cx.sys];
-        const Row4 v = spmv4(S, cx.r0, S.y);
-        const Row4 r0 = ld4(S.r0 + cx.r0);
+    __shared__ int sh[2];
+    NS3D_CHUNK_LOOP
+        if (!sys_active(S)) continue;
+        const Row4 v = spmv4(S, r0, S.y);
+        const Row4 rr0 = ld4(S.r0 + r0);
         double a = 0.0;
 #pragma unroll
         for (int m = 0; m < RPL; ++m)
-            if (cx.r0 + m * LANES < S.n) a = __fma_rn(r0.v[m], v.v[m], a);
-        st4(S.v + cx.r0, v);
-        double t = block_tree_sum(a, sm);
-        if (threadIdx.x == 0) S.part[2 * (size_t)cx.lc] = t;
+            if (r0 + m * LANES < S.n) a = __fma_rn(rr0.v[m], v.v[m], a);
+        st4(S.v + r0, v);
+        const double t = block_tree_sum(a, sm);
+        if (threadIdx.x == 0) S.part[2 * (size_t)lc] = t;
         if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            double d = final_partials_sum(S.part, S.nchunks, 2, sm);
+            const double d = final_partials_sum(S.part, S.nchunks, 2, sm);
             if (threadIdx.x == 0) {
                 S.st->counter = 0;
                 S.st->alpha = S.st->rho / d;
@@ -278,54 +263,47 @@ __global__ void __launch_bounds__(LANES) k_kr_v(const KSys *__restrict__ sys, co
 }
 
 // K3: s = r - alpha v; z = D^-1 s
-__global__ void __launch_bounds__(LANES) k_kr_s(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                int total_chunks) {
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        if (!cx.active) continue;
-        const KSys &S = sys[cx.sys];
+__global__ void __launch_bounds__(LANES) k_kr_s(const __grid_constant__ KSetArg A) {
+    NS3D_CHUNK_LOOP
+        if (!sys_active(S)) continue;
         const double alpha = __ldcg(&S.st->alpha);
-        const Row4 r = ld4(S.r + cx.r0), v = ld4(S.v + cx.r0), iv = ld4(S.invdiag + cx.r0);
+        const Row4 r = ld4(S.r + r0), v = ld4(S.v + r0), iv = ld4(S.invdiag + r0);
         Row4 s, z;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             s.v[m] = __fma_rn(-alpha, v.v[m], r.v[m]);
             z.v[m] = iv.v[m] * s.v[m];
         }
-        st4(S.s + cx.r0, s);
-        st4(S.z + cx.r0, z);
+        st4(S.s + r0, s);
+        st4(S.z + r0, z);
     }
 }
 
 // K4: t = A z, <t, t>, <t, s> -> w
-__global__ void __launch_bounds__(LANES) k_kr_t(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_kr_t(const __grid_constant__ KSetArg A) {
     __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        if (!cx.active) continue;
-        const KSys &S = sys[cx.sys];
-        const Row4 t = spmv4(S, cx.r0, S.z);
-        const Row4 s = ld4(S.s + cx.r0);
+    __shared__ int sh[2];
+    NS3D_CHUNK_LOOP
+        if (!sys_active(S)) continue;
+        const Row4 t = spmv4(S, r0, S.z);
+        const Row4 s = ld4(S.s + r0);
         double att = 0.0, ats = 0.0;
 #pragma unroll
         for (int m = 0; m < RPL; ++m)
-            if (cx.r0 + m * LANES < S.n) {
+            if (r0 + m * LANES < S.n) {
                 att = __fma_rn(t.v[m], t.v[m], att);
                 ats = __fma_rn(t.v[m], s.v[m], ats);
             }
-        st4(S.t + cx.r0, t);
-        double tt = block_tree_sum(att, sm);
-        double ts = block_tree_sum(ats, sm);
+        st4(S.t + r0, t);
+        double tt, ts;
+        block_tree_sum2(att, ats, sm, tt, ts);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = tt;
-            S.part[2 * (size_t)cx.lc + 1] = ts;
+            S.part[2 * (size_t)lc + 0] = tt;
+            S.part[2 * (size_t)lc + 1] = ts;
         }
         if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            double ftt = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            double fts = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double ftt, fts;
+            final_partials_sum2(S.part, S.nchunks, sm, ftt, fts);
             if (threadIdx.x == 0) {
                 S.st->counter = 0;
                 S.st->w = (ftt > 0.0) ? fts / ftt : 0.0;
@@ -335,41 +313,37 @@ __global__ void __launch_bounds__(LANES) k_kr_t(const KSys *__restrict__ sys, co
 }
 
 // K5: x += alpha y + w z; r = s - w t; <r0, r>, <r, r> -> loop control
-__global__ void __launch_bounds__(LANES) k_kr_x(const KSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_kr_x(const __grid_constant__ KSetArg A) {
     __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        ChunkCtx cx = chunk_ctx(sys, chunk_sys, c, sh);
-        if (!cx.active) continue;
-        const KSys &S = sys[cx.sys];
+    __shared__ int sh[2];
+    NS3D_CHUNK_LOOP
+        if (!sys_active(S)) continue;
         const double alpha = __ldcg(&S.st->alpha), w = __ldcg(&S.st->w);
-        const Row4 y = ld4(S.y + cx.r0), z = ld4(S.z + cx.r0), t = ld4(S.t + cx.r0), s = ld4(S.s + cx.r0);
-        const Row4 r0 = ld4(S.r0 + cx.r0);
-        Row4 x = ld4(S.x + cx.r0), r;
+        const Row4 y = ld4(S.y + r0), z = ld4(S.z + r0), t = ld4(S.t + r0), s = ld4(S.s + r0);
+        const Row4 rr0 = ld4(S.r0 + r0);
+        Row4 x = ld4(S.x + r0), r;
         double a0r = 0.0, arr = 0.0;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             x.v[m] = __fma_rn(w, z.v[m], __fma_rn(alpha, y.v[m], x.v[m]));
             r.v[m] = __fma_rn(-w, t.v[m], s.v[m]);
-            if (cx.r0 + m * LANES < S.n) {
-                a0r = __fma_rn(r0.v[m], r.v[m], a0r);
+            if (r0 + m * LANES < S.n) {
+                a0r = __fma_rn(rr0.v[m], r.v[m], a0r);
                 arr = __fma_rn(r.v[m], r.v[m], arr);
             }
         }
-        // x may be a field whose padding is shared with nothing: rows >= n
-        // are written with the values computed from zero padding
-        st4(S.x + cx.r0, x);
-        st4(S.r + cx.r0, r);
-        double t0r = block_tree_sum(a0r, sm);
-        double trr = block_tree_sum(arr, sm);
+        // rows >= n of x are padding; they receive values computed from zeros
+        st4(S.x + r0, x);
+        st4(S.r + r0, r);
+        double t0r, trr;
+        block_tree_sum2(a0r, arr, sm, t0r, trr);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = t0r;
-            S.part[2 * (size_t)cx.lc + 1] = trr;
+            S.part[2 * (size_t)lc + 0] = t0r;
+            S.part[2 * (size_t)lc + 1] = trr;
         }
         if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            double f0r = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            double frr = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double f0r, frr;
+            final_partials_sum2(S.part, S.nchunks, sm, f0r, frr);
             if (threadIdx.x == 0) {
                 KState *st = S.st;
                 st->counter = 0;
@@ -393,38 +367,26 @@ __global__ void __launch_bounds__(LANES) k_kr_x(const KSys *__restrict__ sys, co
 }
 
 // restart of paused systems: r = b - A x, r0 = r, rho = |r0|^2
-__global__ void __launch_bounds__(LANES) k_kr_restart(const KSys *__restrict__ sys,
-                                                      const int *__restrict__ chunk_sys, int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_kr_restart(const __grid_constant__ KSetArg A) {
     __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        if (threadIdx.x == 0) {
-            int s = chunk_sys[c];
-            sh[0] = s;
-            sh[1] = (__ldcg(&sys[s].st->paused) != 0 && __ldcg(&sys[s].st->done) == 0) ? 1 : 0;
-        }
-        __syncthreads();
-        const int sidx = sh[0];
-        const bool act = sh[1] != 0;
-        __syncthreads();
-        if (!act) continue;
-        const KSys &S = sys[sidx];
-        const int lc = c - S.chunk_begin, r0i = lc * CH + threadIdx.x;
-        const Row4 ax = spmv4(S, r0i, S.x);
-        const Row4 b = ld4(S.b + r0i);
+    __shared__ int sh[2];
+    NS3D_CHUNK_LOOP
+        if (!(__ldcg(&S.st->paused) != 0 && __ldcg(&S.st->done) == 0)) continue;
+        const Row4 ax = spmv4(S, r0, S.x);
+        const Row4 b = ld4(S.b + r0);
         Row4 r;
         double arr = 0.0;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             r.v[m] = b.v[m] - ax.v[m];
-            if (r0i + m * LANES < S.n) arr = __fma_rn(r.v[m], r.v[m], arr);
+            if (r0 + m * LANES < S.n) arr = __fma_rn(r.v[m], r.v[m], arr);
         }
-        st4(S.r + r0i, r);
-        st4(S.r0 + r0i, r);
-        double trr = block_tree_sum(arr, sm);
+        st4(S.r + r0, r);
+        st4(S.r0 + r0, r);
+        const double trr = block_tree_sum(arr, sm);
         if (threadIdx.x == 0) S.part[2 * (size_t)lc] = trr;
         if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            double rr = final_partials_sum(S.part, S.nchunks, 2, sm);
+            const double rr = final_partials_sum(S.part, S.nchunks, 2, sm);
             if (threadIdx.x == 0) {
                 KState *st = S.st;
                 st->counter = 0;
@@ -438,14 +400,18 @@ __global__ void __launch_bounds__(LANES) k_kr_restart(const KSys *__restrict__ s
     }
 }
 
-// plain y = A x over one system (tests and diagnostics)
-__global__ void k_spmv(SysView A, const double *__restrict__ x, double *__restrict__ y) {
+#undef NS3D_CHUNK_LOOP
+
+// y = A x for one system (tests and the residual checks of the drivers)
+__global__ void __launch_bounds__(LANES) k_spmv(SysView A, const double *__restrict__ x, double *__restrict__ y) {
     KSys S;
-    S.n = A.n; S.npad = A.npad; S.coef = A.coef; S.nbr = A.nbr;
+    S.n = A.n;
+    S.npad = A.npad;
+    S.coef = A.coef;
+    S.nbr = A.nbr;
     for (int c = blockIdx.x; c < A.nchunks; c += gridDim.x) {
         const int r0 = c * CH + threadIdx.x;
-        const Row4 v = spmv4(S, r0, x);
-        st4(y + r0, v);
+        st4(y + r0, spmv4(S, r0, x));
     }
 }
 
@@ -468,48 +434,47 @@ int device_sm_count() {
 // waves); beyond that, blocks walk the chunks grid-stride
 static inline int kr_grid(int total_chunks) { return std::max(1, std::min(total_chunks, device_sm_count() * 32)); }
 
-void launch_krylov_init(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    (void)nsys;
-    if (total_chunks <= 0) return;
-    count_launches(1); k_kr_init<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    count_launches(1); k_kr_init2<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+void launch_krylov_init(const KSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
+    count_launches(2);
+    k_kr_init<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_kr_init2<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
-void launch_krylov_iteration(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    (void)nsys;
-    if (total_chunks <= 0) return;
-    const int g = kr_grid(total_chunks);
-    count_launches(1); k_kr_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    count_launches(1); k_kr_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    count_launches(1); k_kr_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    count_launches(1); k_kr_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    count_launches(1); k_kr_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+void launch_krylov_iteration(const KSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
+    const int g = kr_grid(A.total_chunks);
+    count_launches(5);
+    k_kr_p<<<g, LANES, 0, st>>>(A);
+    k_kr_v<<<g, LANES, 0, st>>>(A);
+    k_kr_s<<<g, LANES, 0, st>>>(A);
+    k_kr_t<<<g, LANES, 0, st>>>(A);
+    k_kr_x<<<g, LANES, 0, st>>>(A);
 }
 
-void launch_krylov_kernel(int which, const KSys *sys, int nsys, const int *chunk_sys, int total_chunks,
-                          cudaStream_t st) {
-    (void)nsys;
-    if (total_chunks <= 0) return;
-    const int g = kr_grid(total_chunks);
+void launch_krylov_kernel(int which, const KSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
+    const int g = kr_grid(A.total_chunks);
     count_launches(1);
     switch (which) {
-        case 0: k_kr_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
-        case 1: k_kr_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
-        case 2: k_kr_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
-        case 3: k_kr_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
-        default: k_kr_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks); break;
+        case 0: k_kr_p<<<g, LANES, 0, st>>>(A); break;
+        case 1: k_kr_v<<<g, LANES, 0, st>>>(A); break;
+        case 2: k_kr_s<<<g, LANES, 0, st>>>(A); break;
+        case 3: k_kr_t<<<g, LANES, 0, st>>>(A); break;
+        default: k_kr_x<<<g, LANES, 0, st>>>(A); break;
     }
 }
 
-void launch_krylov_restart(const KSys *sys, int nsys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    (void)nsys;
-    if (total_chunks <= 0) return;
-    count_launches(1); k_kr_restart<<<kr_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+void launch_krylov_restart(const KSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
+    count_launches(1);
+    k_kr_restart<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st) {
     if (A.n <= 0) return;
-    count_launches(1); k_spmv<<<std::max(1, std::min(A.nchunks, device_sm_count() * 6)), LANES, 0, st>>>(A, x, y);
+    count_launches(1);
+    k_spmv<<<std::max(1, std::min(A.nchunks, device_sm_count() * 6)), LANES, 0, st>>>(A, x, y);
 }
 
 }  // namespace ns3d

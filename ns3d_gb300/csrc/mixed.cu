@@ -63,30 +63,30 @@ __device__ __forceinline__ double spmv_f64_row(const MSys &S, int row, const dou
                        [&](double acc, int s, int col) { return __fma_rn(cf[(size_t)s * np], x[col], acc); });
 }
 
-struct MCtx {
-    int sys, lc, r0;
-    bool active;
-};
-
-// active: the outer loop is running and (if `inner`) the inner solve too
-__device__ __forceinline__ MCtx mctx(const MSys *sys, const int *chunk_sys, int c, int *sh, bool inner) {
-    MCtx cx;
-    if (threadIdx.x == 0) {
-        int s = chunk_sys[c];
-        const MSys &S = sys[s];
-        int act = __ldcg(&S.dc->done) == 0;
-        if (inner) act = act && __ldcg(&S.st->done) == 0;
-        sh[0] = s;
-        sh[1] = act;
-    }
-    __syncthreads();
-    cx.sys = sh[0];
-    cx.active = sh[1] != 0;
-    __syncthreads();
-    cx.lc = c - sys[cx.sys].chunk_begin;
-    cx.r0 = cx.lc * CH + threadIdx.x;
-    return cx;
+// system owning global chunk c (systems in chunk order, first begins at 0)
+__device__ __forceinline__ int msys_of_chunk(const MSetArg &A, int c) {
+    int s = 0;
+#pragma unroll
+    for (int q = 1; q < KMAX; ++q)
+        if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
+    return s;
 }
+
+// Flags change only between kernels (or in the last block of a system, after
+// every other block of that system has passed its check), so all threads of a
+// block read the same values.  `inner`: the FP32 solve must be running too.
+__device__ __forceinline__ bool m_active(const MSys &S, bool inner) {
+    bool act = __ldcg(&S.dc->done) == 0;
+    if (inner) act = act && __ldcg(&S.st->done) == 0;
+    return act;
+}
+
+#define NS3D_MCHUNK_LOOP(INNER)                                              \
+    for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {           \
+        const MSys &S = A.sys[msys_of_chunk(A, c)];                          \
+        if (!m_active(S, INNER)) continue;                                    \
+        const int lc = c - S.chunk_begin;                                     \
+        const int r0 = lc * CH + threadIdx.x;
 
 __device__ __forceinline__ bool m_arrive_last(unsigned int *counter, unsigned int total, int *sh) {
     __syncthreads();
@@ -104,18 +104,14 @@ __device__ __forceinline__ bool m_arrive_last(unsigned int *counter, unsigned in
 __device__ __forceinline__ bool finite(double x) { return isfinite(x); }
 
 // ---- FP64 residual and outer control -----------------------------------------
-__global__ void __launch_bounds__(LANES) k_dc_resid(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                    int total_chunks, int first) {
+__global__ void __launch_bounds__(LANES) k_dc_resid(const __grid_constant__ MSetArg A, int first) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, false);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(false)
         double arr = 0.0, abb = 0.0;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
-            const int row = cx.r0 + m * LANES;
+            const int row = r0 + m * LANES;
             const double b = S.b64[row];
             const double r = b - spmv_f64_row(S, row, S.x64);
             S.r64[row] = r;
@@ -124,15 +120,15 @@ __global__ void __launch_bounds__(LANES) k_dc_resid(const MSys *__restrict__ sys
                 abb = __fma_rn(b, b, abb);
             }
         }
-        const double trr = block_tree_sum(arr, sm);
-        const double tbb = block_tree_sum(abb, sm);
+        double trr, tbb;
+        block_tree_sum2(arr, abb, sm, trr, tbb);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = trr;
-            S.part[2 * (size_t)cx.lc + 1] = tbb;
+            S.part[2 * (size_t)lc + 0] = trr;
+            S.part[2 * (size_t)lc + 1] = tbb;
         }
         if (m_arrive_last(&S.dc->counter, (unsigned)S.nchunks, sh)) {
-            const double rr = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            const double bb = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double rr, bb;
+            final_partials_sum2(S.part, S.nchunks, sm, rr, bb);
             if (threadIdx.x == 0) {
                 DCState *dc = S.dc;
                 KState *st = S.st;
@@ -174,18 +170,10 @@ __global__ void __launch_bounds__(LANES) k_dc_resid(const MSys *__restrict__ sys
 }
 
 // x64 = 0 for systems with a zero right-hand side (first round)
-__global__ void k_dc_zero(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys, int total_chunks) {
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        if (threadIdx.x == 0) {
-            sh[0] = chunk_sys[c];
-            sh[1] = __ldcg(&sys[sh[0]].dc->zero_rhs);
-        }
-        __syncthreads();
-        const int s = sh[0], z = sh[1];
-        __syncthreads();
-        if (!z) continue;
-        const MSys &S = sys[s];
+__global__ void k_dc_zero(const __grid_constant__ MSetArg A) {
+    for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
+        const MSys &S = A.sys[msys_of_chunk(A, c)];
+        if (!__ldcg(&S.dc->zero_rhs)) continue;
         const int r0 = (c - S.chunk_begin) * CH + threadIdx.x;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) S.x64[r0 + m * LANES] = 0.0;
@@ -193,14 +181,10 @@ __global__ void k_dc_zero(const MSys *__restrict__ sys, const int *__restrict__ 
 }
 
 // ---- FP32 inner solve -------------------------------------------------------
-__global__ void __launch_bounds__(LANES) k_m32_init(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                    int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSetArg A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         const double scale = __ldcg(&S.dc->scale);
         float acc = 0.0f;
         RowF4 f;
@@ -209,17 +193,17 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const MSys *__restrict__ sys
         for (int m = 0; m < RPL; ++m) zero.v[m] = 0.0f;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
-            const int row = cx.r0 + m * LANES;
+            const int row = r0 + m * LANES;
             f.v[m] = (float)(S.r64[row] * scale);
             if (row < S.n) acc = __fmaf_rn(f.v[m], f.v[m], acc);
         }
-        stf4(S.r + cx.r0, f);
-        stf4(S.r0 + cx.r0, f);
-        stf4(S.x + cx.r0, zero);
-        stf4(S.p + cx.r0, zero);
-        stf4(S.v + cx.r0, zero);
+        stf4(S.r + r0, f);
+        stf4(S.r0 + r0, f);
+        stf4(S.x + r0, zero);
+        stf4(S.p + r0, zero);
+        stf4(S.v + r0, zero);
         const double t = block_tree_sum((double)acc, sm);
-        if (threadIdx.x == 0) S.part[2 * (size_t)cx.lc] = t;
+        if (threadIdx.x == 0) S.part[2 * (size_t)lc] = t;
         if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
             const double bb = final_partials_sum(S.part, S.nchunks, 2, sm);
             if (threadIdx.x == 0) {
@@ -244,44 +228,36 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const MSys *__restrict__ sys
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_p(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                 int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_p(const __grid_constant__ MSetArg A) {
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         const float beta = (float)__ldcg(&S.st->beta), w = (float)__ldcg(&S.st->w);
-        const RowF4 r = ldf4(S.r + cx.r0), v = ldf4(S.v + cx.r0), iv = ldf4(S.invdiag32 + cx.r0);
-        RowF4 p = ldf4(S.p + cx.r0), y;
+        const RowF4 r = ldf4(S.r + r0), v = ldf4(S.v + r0), iv = ldf4(S.invdiag32 + r0);
+        RowF4 p = ldf4(S.p + r0), y;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             p.v[m] = __fmaf_rn(beta, __fmaf_rn(-w, v.v[m], p.v[m]), r.v[m]);
             y.v[m] = iv.v[m] * p.v[m];
         }
-        stf4(S.p + cx.r0, p);
-        stf4(S.y + cx.r0, y);
+        stf4(S.p + r0, p);
+        stf4(S.y + r0, y);
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_v(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                 int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_v(const __grid_constant__ MSetArg A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         float a = 0.0f;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
-            const int row = cx.r0 + m * LANES;
+            const int row = r0 + m * LANES;
             const float v = spmv_f32_row(S, row, S.y);
             S.v[row] = v;
             if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
         }
         const double t = block_tree_sum((double)a, sm);
-        if (threadIdx.x == 0) S.part[2 * (size_t)cx.lc] = t;
+        if (threadIdx.x == 0) S.part[2 * (size_t)lc] = t;
         if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
             const double d = final_partials_sum(S.part, S.nchunks, 2, sm);
             if (threadIdx.x == 0) {
@@ -292,38 +268,30 @@ __global__ void __launch_bounds__(LANES) k_m32_v(const MSys *__restrict__ sys, c
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_s(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                 int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_s(const __grid_constant__ MSetArg A) {
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         const float alpha = (float)__ldcg(&S.st->alpha);
-        const RowF4 r = ldf4(S.r + cx.r0), v = ldf4(S.v + cx.r0), iv = ldf4(S.invdiag32 + cx.r0);
+        const RowF4 r = ldf4(S.r + r0), v = ldf4(S.v + r0), iv = ldf4(S.invdiag32 + r0);
         RowF4 s, z;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             s.v[m] = __fmaf_rn(-alpha, v.v[m], r.v[m]);
             z.v[m] = iv.v[m] * s.v[m];
         }
-        stf4(S.s + cx.r0, s);
-        stf4(S.z + cx.r0, z);
+        stf4(S.s + r0, s);
+        stf4(S.z + r0, z);
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_t(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                 int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_t(const __grid_constant__ MSetArg A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         float att = 0.0f, ats = 0.0f;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
-            const int row = cx.r0 + m * LANES;
+            const int row = r0 + m * LANES;
             const float t = spmv_f32_row(S, row, S.z);
             S.t[row] = t;
             if (row < S.n) {
@@ -331,15 +299,15 @@ __global__ void __launch_bounds__(LANES) k_m32_t(const MSys *__restrict__ sys, c
                 ats = __fmaf_rn(t, S.s[row], ats);
             }
         }
-        const double tt = block_tree_sum((double)att, sm);
-        const double ts = block_tree_sum((double)ats, sm);
+        double tt, ts;
+        block_tree_sum2((double)att, (double)ats, sm, tt, ts);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = tt;
-            S.part[2 * (size_t)cx.lc + 1] = ts;
+            S.part[2 * (size_t)lc + 0] = tt;
+            S.part[2 * (size_t)lc + 1] = ts;
         }
         if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
-            const double ftt = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            const double fts = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double ftt, fts;
+            final_partials_sum2(S.part, S.nchunks, sm, ftt, fts);
             if (threadIdx.x == 0) {
                 S.st->counter = 0;
                 S.st->w = (ftt > 0.0) ? fts / ftt : 0.0;
@@ -348,39 +316,35 @@ __global__ void __launch_bounds__(LANES) k_m32_t(const MSys *__restrict__ sys, c
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_x(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys,
-                                                 int total_chunks) {
+__global__ void __launch_bounds__(LANES) k_m32_x(const __grid_constant__ MSetArg A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        MCtx cx = mctx(sys, chunk_sys, c, sh, true);
-        if (!cx.active) continue;
-        const MSys &S = sys[cx.sys];
+    NS3D_MCHUNK_LOOP(true)
         const float alpha = (float)__ldcg(&S.st->alpha), w = (float)__ldcg(&S.st->w);
-        const RowF4 y = ldf4(S.y + cx.r0), z = ldf4(S.z + cx.r0), t = ldf4(S.t + cx.r0), s = ldf4(S.s + cx.r0);
-        const RowF4 r0 = ldf4(S.r0 + cx.r0);
-        RowF4 x = ldf4(S.x + cx.r0), r;
+        const RowF4 y = ldf4(S.y + r0), z = ldf4(S.z + r0), t = ldf4(S.t + r0), s = ldf4(S.s + r0);
+        const RowF4 rr0 = ldf4(S.r0 + r0);
+        RowF4 x = ldf4(S.x + r0), r;
         float a0r = 0.0f, arr = 0.0f;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             x.v[m] = __fmaf_rn(w, z.v[m], __fmaf_rn(alpha, y.v[m], x.v[m]));
             r.v[m] = __fmaf_rn(-w, t.v[m], s.v[m]);
-            if (cx.r0 + m * LANES < S.n) {
-                a0r = __fmaf_rn(r0.v[m], r.v[m], a0r);
+            if (r0 + m * LANES < S.n) {
+                a0r = __fmaf_rn(rr0.v[m], r.v[m], a0r);
                 arr = __fmaf_rn(r.v[m], r.v[m], arr);
             }
         }
-        stf4(S.x + cx.r0, x);
-        stf4(S.r + cx.r0, r);
-        const double t0r = block_tree_sum((double)a0r, sm);
-        const double trr = block_tree_sum((double)arr, sm);
+        stf4(S.x + r0, x);
+        stf4(S.r + r0, r);
+        double t0r, trr;
+        block_tree_sum2((double)a0r, (double)arr, sm, t0r, trr);
         if (threadIdx.x == 0) {
-            S.part[2 * (size_t)cx.lc + 0] = t0r;
-            S.part[2 * (size_t)cx.lc + 1] = trr;
+            S.part[2 * (size_t)lc + 0] = t0r;
+            S.part[2 * (size_t)lc + 1] = trr;
         }
         if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
-            const double f0r = final_partials_sum(S.part + 0, S.nchunks, 2, sm);
-            const double frr = final_partials_sum(S.part + 1, S.nchunks, 2, sm);
+            double f0r, frr;
+            final_partials_sum2(S.part, S.nchunks, sm, f0r, frr);
             if (threadIdx.x == 0) {
                 KState *st = S.st;
                 st->counter = 0;
@@ -404,19 +368,10 @@ __global__ void __launch_bounds__(LANES) k_m32_x(const MSys *__restrict__ sys, c
     }
 }
 
-__global__ void k_dc_update(const MSys *__restrict__ sys, const int *__restrict__ chunk_sys, int total_chunks) {
-    __shared__ int sh[4];
-    for (int c = blockIdx.x; c < total_chunks; c += gridDim.x) {
-        if (threadIdx.x == 0) {
-            const int s = chunk_sys[c];
-            sh[0] = s;
-            sh[1] = __ldcg(&sys[s].dc->done) == 0 && __ldcg(&sys[s].st->info) == 0;
-        }
-        __syncthreads();
-        const int s = sh[0], act = sh[1];
-        __syncthreads();
-        if (!act) continue;
-        const MSys &S = sys[s];
+__global__ void k_dc_update(const __grid_constant__ MSetArg A) {
+    for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
+        const MSys &S = A.sys[msys_of_chunk(A, c)];
+        if (!(__ldcg(&S.dc->done) == 0 && __ldcg(&S.st->info) == 0)) continue;
         const double inv = 1.0 / __ldcg(&S.dc->scale);
         const int r0 = (c - S.chunk_begin) * CH + threadIdx.x;
 #pragma unroll
@@ -426,6 +381,8 @@ __global__ void k_dc_update(const MSys *__restrict__ sys, const int *__restrict_
         }
     }
 }
+
+#undef NS3D_MCHUNK_LOOP
 
 // FP32 copy of a system's coefficients and inverse diagonal
 __global__ void k_to_f32(const double *__restrict__ coef, const double *__restrict__ invdiag, int npad,
@@ -448,37 +405,37 @@ void launch_to_f32(const double *coef, const double *invdiag, int npad, float *c
                                                                                 invdiag32);
 }
 
-void launch_dc_resid(const MSys *sys, const int *chunk_sys, int total_chunks, int first, cudaStream_t st) {
-    if (total_chunks <= 0) return;
+void launch_dc_resid(const MSetArg &A, int first, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_dc_resid<<<m_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks, first);
+    k_dc_resid<<<m_grid(A.total_chunks), LANES, 0, st>>>(A, first);
     if (first) {
         count_launches(1);
-        k_dc_zero<<<m_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+        k_dc_zero<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
     }
 }
 
-void launch_m32_init(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    if (total_chunks <= 0) return;
+void launch_m32_init(const MSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_m32_init<<<m_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    k_m32_init<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
-void launch_m32_iteration(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    if (total_chunks <= 0) return;
-    const int g = m_grid(total_chunks);
+void launch_m32_iteration(const MSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
+    const int g = m_grid(A.total_chunks);
     count_launches(5);
-    k_m32_p<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_m32_v<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_m32_s<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_m32_t<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
-    k_m32_x<<<g, LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    k_m32_p<<<g, LANES, 0, st>>>(A);
+    k_m32_v<<<g, LANES, 0, st>>>(A);
+    k_m32_s<<<g, LANES, 0, st>>>(A);
+    k_m32_t<<<g, LANES, 0, st>>>(A);
+    k_m32_x<<<g, LANES, 0, st>>>(A);
 }
 
-void launch_dc_update(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st) {
-    if (total_chunks <= 0) return;
+void launch_dc_update(const MSetArg &A, cudaStream_t st) {
+    if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_dc_update<<<m_grid(total_chunks), LANES, 0, st>>>(sys, chunk_sys, total_chunks);
+    k_dc_update<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
 }  // namespace ns3d

@@ -26,11 +26,17 @@ struct MSys {
     DCState *dc;
 };
 
+// A mixed solve set as a kernel argument (by value; systems in chunk order)
+struct MSetArg {
+    int nsys, total_chunks;
+    MSys sys[KMAX];
+};
+
 void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
                    cudaStream_t st);
-void launch_dc_resid(const MSys *sys, const int *chunk_sys, int total_chunks, int first, cudaStream_t st);
-void launch_m32_init(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
-void launch_m32_iteration(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
-void launch_dc_update(const MSys *sys, const int *chunk_sys, int total_chunks, cudaStream_t st);
+void launch_dc_resid(const MSetArg &set, int first, cudaStream_t st);
+void launch_m32_init(const MSetArg &set, cudaStream_t st);
+void launch_m32_iteration(const MSetArg &set, cudaStream_t st);
+void launch_dc_update(const MSetArg &set, cudaStream_t st);
 
 }  // namespace ns3d

@@ -22,6 +22,7 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     }
     if (key == key_) return;
     const int ns = (int)items.size();
+    if (ns > KMAX) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     std::vector<MSys> ms(ns);
     int chunk = 0;
     if ((int)st_.n < ns) {
@@ -31,8 +32,6 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
         h_st_.alloc(ns);
         h_out_.alloc(ns);
         h_dc_.alloc(ns);
-        h_msys_.alloc(ns);
-        msys_.alloc(ns);
     }
     for (int i = 0; i < ns; ++i) {
         DevSys &S = *items[i].sys;
@@ -57,14 +56,11 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
         m.st = st_.p + i;
         m.dc = dc_.p + i;
     }
-    std::memcpy(h_msys_.p, ms.data(), ns * sizeof(MSys));
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(msys_.p, h_msys_.p, ns * sizeof(MSys), cudaMemcpyHostToDevice, st));
-    std::vector<int> cs((size_t)std::max(chunk, 1));
-    for (int i = 0; i < ns; ++i)
-        for (int c = 0; c < ms[i].nchunks; ++c) cs[(size_t)ms[i].chunk_begin + c] = i;
-    chunk_sys_.alloc(cs.size());
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(chunk_sys_.p, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+    std::memset(&set_, 0, sizeof set_);
+    set_.nsys = ns;
+    set_.total_chunks = chunk;
+    for (int i = 0; i < ns; ++i) set_.sys[i] = ms[i];
+    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));  // FP32 buffers allocated above
     key_ = key;
     nsys_ = ns;
     total_chunks_ = chunk;
@@ -96,7 +92,7 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
     }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(dc_.p, h_dc_.p, ns * sizeof(DCState), cudaMemcpyHostToDevice, st));
     NS3D_CUDA_CHECK(cudaMemcpyAsync(st_.p, h_st_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
-    launch_dc_resid(msys_.p, chunk_sys_.p, total_chunks_, 1, st);
+    launch_dc_resid(set_, 1, st);
     // Every round runs at least one inner iteration per unfinished system, so
     // maxit + 2 rounds bound the loop; each round's inner loop is bounded by
     // the remaining iteration budget.
@@ -110,11 +106,11 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
         for (int i = 0; i < ns; ++i) all_done = all_done && h_dc_.p[i].done;
         if (all_done) break;
         if (++rounds > maxit + 2L) throw ApiError(NS3D_ERR_TIMEOUT, "defect correction exceeded its round bound");
-        launch_m32_init(msys_.p, chunk_sys_.p, total_chunks_, st);
+        launch_m32_init(set_, st);
         long issued = 0;
         int batch = std::max(1, std::min(32, prev_iters_ / 2));
         while (true) {
-            for (int b = 0; b < batch; ++b) launch_m32_iteration(msys_.p, chunk_sys_.p, total_chunks_, st);
+            for (int b = 0; b < batch; ++b) launch_m32_iteration(set_, st);
             issued += batch;
             batch = std::min(64, batch * 2);
             NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
@@ -129,8 +125,8 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
         for (int i = 0; i < ns; ++i)
             if (!h_dc_.p[i].done) round_max = std::max(round_max, h_st_.p[i].iter);
         prev_iters_ = std::max(2, round_max);
-        launch_dc_update(msys_.p, chunk_sys_.p, total_chunks_, st);
-        launch_dc_resid(msys_.p, chunk_sys_.p, total_chunks_, 0, st);
+        launch_dc_update(set_, st);
+        launch_dc_resid(set_, 0, st);
     }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
     NS3D_CUDA_CHECK(cudaStreamSynchronize(st));

@@ -31,11 +31,9 @@ constexpr int kScratchChunks = kScratchRows / CH;
 constexpr int kVectors = 9;  // r, r0, p, v, y, s, z, t, invdiag
 constexpr size_t kVecBytes = (size_t)kVectors * kScratchRows * sizeof(double);
 constexpr size_t kPartBytes = (size_t)2 * kScratchChunks * sizeof(double);
-constexpr size_t kSysOffset = kVecBytes + kPartBytes;
-constexpr size_t kStateOffset = kSysOffset + 256;
-constexpr size_t kChunkOffset = kStateOffset + 256;
-constexpr size_t kScratchBytes = kChunkOffset + (size_t)kScratchChunks * sizeof(int);
-static_assert(sizeof(KSys) <= 256 && sizeof(KState) <= 256, "scratch layout");
+constexpr size_t kStateOffset = kVecBytes + kPartBytes;
+constexpr size_t kScratchBytes = kStateOffset + 256;
+static_assert(sizeof(KState) <= 256, "scratch layout");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -100,13 +98,14 @@ extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t 
     if (rc != NS3D_OK) return fail(rc, "cudaGetSymbolAddress failed for the scratch array");
     double *vec = (double *)base;
     double *part = (double *)(base + kVecBytes);
-    KSys *dsys = (KSys *)(base + kSysOffset);
     KState *dst = (KState *)(base + kStateOffset);
-    int *dchunk = (int *)(base + kChunkOffset);
     const int nchunks = (n + CH - 1) / CH;
 
-    KSys hs;
-    std::memset(&hs, 0, sizeof hs);
+    KSetArg set;
+    std::memset(&set, 0, sizeof set);
+    set.nsys = 1;
+    set.total_chunks = nchunks;
+    KSys &hs = set.sys[0];
     hs.n = n;
     hs.npad = npad;
     hs.nchunks = nchunks;
@@ -127,17 +126,15 @@ extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t 
     k0.maxit = maxit;
 
     auto ok = [](cudaError_t e) { return e == cudaSuccess; };
-    // the scratch keeps the previous call's contents: state, counter, chunk
-    // table and the inverse diagonal are rewritten here, p and v are zeroed
-    // by the init kernels
-    if (!ok(cudaMemcpyAsync(dsys, &hs, sizeof hs, cudaMemcpyHostToDevice, st)) ||
-        !ok(cudaMemcpyAsync(dst, &k0, sizeof k0, cudaMemcpyHostToDevice, st)) ||
-        !ok(cudaMemsetAsync(dchunk, 0, (size_t)nchunks * sizeof(int), st)) ||
+    // the scratch keeps the previous call's contents: state, counter and the
+    // inverse diagonal are rewritten here, p and v are zeroed by the init
+    // kernels; the system's pointers travel as a kernel argument
+    if (!ok(cudaMemcpyAsync(dst, &k0, sizeof k0, cudaMemcpyHostToDevice, st)) ||
         !ok(cudaMemsetAsync(invdiag, 0, (size_t)nchunks * CH * sizeof(double), st)))
         return fail(NS3D_ERR_CUDA, "scratch set-up copy failed");
     k_noalloc_invdiag<<<std::max(1, std::min((n + 255) / 256, 1024)), 256, 0, st>>>(coef, n, invdiag);
     count_launches(1);
-    launch_krylov_init(dsys, 1, dchunk, nchunks, st);
+    launch_krylov_init(set, st);
     const long cap = 2L * maxit + 64;
     long issued = 0;
     int batch = 4;
@@ -147,8 +144,8 @@ extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t 
             return fail(NS3D_ERR_CUDA, "CUDA error while solving (see cudaGetLastError)");
         if (h.done) break;
         if (issued >= cap) return fail(NS3D_ERR_TIMEOUT, "BiCGSTAB exceeded its iteration bound");
-        if (h.paused) launch_krylov_restart(dsys, 1, dchunk, nchunks, st);
-        for (int b = 0; b < batch; ++b) launch_krylov_iteration(dsys, 1, dchunk, nchunks, st);
+        if (h.paused) launch_krylov_restart(set, st);
+        for (int b = 0; b < batch; ++b) launch_krylov_iteration(set, st);
         issued += batch;
         batch = std::min(64, batch * 2);
     }

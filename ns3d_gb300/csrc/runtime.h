@@ -10,6 +10,7 @@
 #include "../../include/ns3d_capi.h"
 #include "device.cuh"
 #include "kernels.h"
+#include "mixed.h"
 
 namespace ns3d {
 
@@ -145,18 +146,14 @@ class KrylovSet {
     void issue_batch(int batch, cudaStream_t st);
     void collect_batch(int batch, const std::vector<int> &work_before);
     std::vector<cudaEvent_t> events_;
-    DBuf<KSys> ksys_;
-    DBuf<int> chunk_sys_;
+    KSetArg set_;  // passed to every kernel by value
     DBuf<KState> st_;
     HBuf<KState> h_st_, h_up_;
-    HBuf<KSys> h_ksys_;
-    std::vector<KSys> cur_;
     int nsys_ = 0, total_chunks_ = 0;
     int prev_iters_ = 8;
     long launches_ = 0;
 };
 
-struct MSys;
 struct DCState;
 
 // A set of systems solved by FP32 BiCGSTAB inside FP64 defect correction.
@@ -173,14 +170,12 @@ class MixedSet {
 
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
-    DBuf<MSys> msys_;
-    DBuf<int> chunk_sys_;
     DBuf<KState> st_, out_st_;
     DBuf<DCState> dc_;
     HBuf<KState> h_st_, h_out_;
     HBuf<DCState> h_dc_;
-    HBuf<MSys> h_msys_;
     std::vector<const double *> key_;
+    MSetArg set_;  // passed to every kernel by value
     int nsys_ = 0, total_chunks_ = 0;
     int prev_iters_ = 8;
 };

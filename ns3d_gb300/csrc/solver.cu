@@ -71,28 +71,19 @@ void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) 
         ks.push_back(k);
     }
     const int ns = (int)ks.size();
-    bool same = ns == nsys_ && chunk == total_chunks_ && cur_.size() == ks.size();
-    if (same)
-        for (int i = 0; i < ns; ++i)
-            if (std::memcmp(&cur_[i], &ks[i], sizeof(KSys) - sizeof(KState *)) != 0) same = false;
-    if (same) return;
+    if (ns > KMAX) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     if ((int)st_.n < ns) {
         st_.alloc_zero(ns, st);
         h_st_.alloc(ns);
         h_up_.alloc(ns);
-        h_ksys_.alloc(ns);
     }
-    for (int i = 0; i < ns; ++i) ks[i].st = st_.p + i;
-    if ((int)ksys_.n < ns) ksys_.alloc(ns);
-    std::memcpy(h_ksys_.p, ks.data(), ns * sizeof(KSys));
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(ksys_.p, h_ksys_.p, ns * sizeof(KSys), cudaMemcpyHostToDevice, st));
-    std::vector<int> cs((size_t)std::max(chunk, 1));
-    for (int i = 0; i < ns; ++i)
-        for (int c = 0; c < ks[i].nchunks; ++c) cs[(size_t)ks[i].chunk_begin + c] = i;
-    chunk_sys_.alloc(cs.size());
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(chunk_sys_.p, cs.data(), cs.size() * sizeof(int), cudaMemcpyHostToDevice, st));
-    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));  // cs is a host temporary
-    cur_ = ks;
+    std::memset(&set_, 0, sizeof set_);
+    set_.nsys = ns;
+    set_.total_chunks = chunk;
+    for (int i = 0; i < ns; ++i) {
+        ks[i].st = st_.p + i;
+        set_.sys[i] = ks[i];
+    }
     nsys_ = ns;
     total_chunks_ = chunk;
 }
@@ -117,7 +108,7 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
         maxit = std::max(maxit, items[i].maxit);
     }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(st_.p, h_up_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
-    launch_krylov_init(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+    launch_krylov_init(set_, st);
     launches_ += 2;
     // Iterations are issued in batches; finished systems make the kernels
     // return at once, so a batch may overshoot the last iteration harmlessly.
@@ -140,7 +131,7 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
         if (all_done) break;
         if (issued >= cap) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
         if (any_paused) {
-            launch_krylov_restart(ksys_.p, ns, chunk_sys_.p, total_chunks_, st);
+            launch_krylov_restart(set_, st);
             launches_ += 1;
         }
         issue_batch(batch, st);
@@ -167,7 +158,7 @@ KrylovSet::~KrylovSet() {
 
 void KrylovSet::issue_batch(int batch, cudaStream_t st) {
     if (!profiling) {
-        for (int b = 0; b < batch; ++b) launch_krylov_iteration(ksys_.p, nsys_, chunk_sys_.p, total_chunks_, st);
+        for (int b = 0; b < batch; ++b) launch_krylov_iteration(set_, st);
         return;
     }
     const size_t need = (size_t)batch * 5 + 1;
@@ -179,7 +170,7 @@ void KrylovSet::issue_batch(int batch, cudaStream_t st) {
     NS3D_CUDA_CHECK(cudaEventRecord(events_[0], st));
     for (int b = 0; b < batch; ++b)
         for (int k = 0; k < 5; ++k) {
-            launch_krylov_kernel(k, ksys_.p, nsys_, chunk_sys_.p, total_chunks_, st);
+            launch_krylov_kernel(k, set_, st);
             NS3D_CUDA_CHECK(cudaEventRecord(events_[(size_t)b * 5 + k + 1], st));
         }
 }
@@ -188,7 +179,7 @@ void KrylovSet::collect_batch(int batch, const std::vector<int> &work_before) {
     for (int b = 0; b < batch; ++b) {
         int64_t rows = 0;
         for (int i = 0; i < nsys_; ++i)
-            if (h_st_.p[i].work - work_before[i] > b) rows += cur_[i].n;
+            if (h_st_.p[i].work - work_before[i] > b) rows += set_.sys[i].n;
         for (int k = 0; k < 5; ++k) {
             float ms = 0;
             NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, events_[(size_t)b * 5 + k], events_[(size_t)b * 5 + k + 1]));
