@@ -11,10 +11,12 @@ permeability solve; steps cycle through SIMPLEC, SIMPLER (N1=2), SIMPLERR
          resets the fields on the device and solves)
   e2e    solves/s through the C-ABI with host buffers: every step uploads the
          raw voxel image, builds the geometry, solves and downloads the fields
-  roofline  the Krylov SpMV kernels (K2 v = A y + <r0,v>, K4 t = A z +
-         <t,t>,<t,s>) of the pressure(-correction) solves: algorithmic bytes
-         (104 B per row: 7 coefficients, 6 neighbour indices, the gathered
-         vector, the fused-dot operand, the result) over their CUDA-event time
+  roofline  the BiCGSTAB loop kernel (one persistent cooperative launch runs
+         the iterations of a solve: K1 p/y, K2 v = A y + <r0,v>, K3 s/z,
+         K4 t = A z + <t,t>,<t,s>, K5 x/r + <r0,r>,<r,r>) of the
+         pressure(-correction) solves: algorithmic bytes per row-iteration
+         (360 B: each vector element and matrix entry read or written once)
+         over the kernel's CUDA-event time
   cpu_baseline  the CPU oracle (the repo's restatement of the reference solver)
          on the first outer iterations of the same solve with every host core,
          scaled to a full solve by BiCGSTAB row-iterations
@@ -43,7 +45,17 @@ sys.path.insert(0, ROOT)
 METHODS = ["SIMPLEC", "SIMPLER", "SIMPLERR", "IDEAL"]
 SHAPE = (128, 128, 128)
 RADIUS, TARGET_PHI, SEED = 8, 0.5, 1
-SPMV_BYTES_PER_ROW = 104  # 7*8 coefficients + 6*4 indices + 8 gathered x + 8 dot operand + 8 result
+# algorithmic bytes of one BiCGSTAB iteration per row: K1 48 (r, v, p, D^-1 in;
+# p, y out), K2 104 (7 coefficients, 6 indices, gathered y, r0 in; v out),
+# K3 40 (r, v, D^-1 in; s, z out), K4 104 (as K2 with z, s; t out), K5 64
+# (y, z, t, s, r0, x in; x, r out)
+LOOP_BYTES_PER_ROW = 360
+# FP64 instructions per row-iteration (a full 7-point row): two SpMVs (7 fma
+# each), five dot-product fma, vector updates p 2, y 1, s 1, z 1, x 2, r 1
+LOOP_FP64_PER_ROW = 27
+# FP64 FMA throughput of this GPU, measured with a dependent-chain-free FMA
+# loop over every SM (the tensor-core FP64 rate of GB300 is not used here)
+FP64_PEAK_TFLOPS = 1.2
 
 # BiCGSTAB row-iterations of one complete solve of this workload per method,
 # measured by this benchmark's GPU arm; the CPU oracle follows the same
@@ -78,11 +90,11 @@ def load_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per SpMV launch from the committed ncu summary, if any."""
-    path = os.path.join(ROOT, "profiles", "krylov_spmv_fp64_128.md")
+    """DRAM bytes per row-iteration of the loop kernel from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "krylov_loop_fp64_128.md")
     try:
         for line in open(path):
-            if line.startswith("dram_bytes_per_launch_full_size:"):
+            if line.startswith("dram_bytes_per_row_iteration:"):
                 return float(line.split(":")[1])
     except OSError:
         pass
@@ -253,11 +265,10 @@ def run_gpu(args):
             tot["launches"][k] += p.launches[k]
             tot["rows"][k] += p.rows[k]
         s.set_profiling(False)
-    spmv_ms = tot["ms"][1] + tot["ms"][3]
-    spmv_launches = tot["launches"][1] + tot["launches"][3]
-    spmv_rows = tot["rows"][1] + tot["rows"][3]
+    loop_ms, loop_launches, loop_rows = tot["ms"][5], tot["launches"][5], tot["rows"][5]
     peak, peak_kind = load_peaks()
-    achieved = SPMV_BYTES_PER_ROW * spmv_rows / (spmv_ms * 1e-3) / 1e9 if spmv_ms > 0 else 0.0
+    achieved = LOOP_BYTES_PER_ROW * loop_rows / (loop_ms * 1e-3) / 1e9 if loop_ms > 0 else 0.0
+    fp64_tflops = LOOP_FP64_PER_ROW * loop_rows / (loop_ms * 1e-3) / 1e12 if loop_ms > 0 else 0.0
     traffic = ncu_traffic()
     kr_rows = {METHODS[i % len(METHODS)]: int(results[i].krylov_rows) for i in range(len(results))}
     outer_its = {METHODS[i % len(METHODS)]: int(results[i].iterations) for i in range(len(results))}
@@ -303,14 +314,19 @@ def run_gpu(args):
                            "cell_updates_per_s": cell_updates / elapsed * world},
                 "e2e": {"value": e2e_value, "unit": "solves/s", "h2d_bytes_per_step": h2d,
                         "d2h_bytes_per_step": d2h},
-                "roofline": {"bound": "hbm", "kernel": "krylov SpMV K2+K4 (pressure solves)",
+                "roofline": {"bound": "hbm", "kernel": "k_kr_loop (BiCGSTAB iterations of the pressure solves)",
                              "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                             "peak_kind": peak_kind, "traffic": traffic,
-                             "bytes_per_row": SPMV_BYTES_PER_ROW,
-                             "avg_launch_us": 1000.0 * spmv_ms / max(spmv_launches, 1),
-                             "rows_per_launch": spmv_rows / max(spmv_launches, 1)},
-                "kernels": {n: {"launches": tot["launches"][k], "ms": round(tot["ms"][k], 3)}
-                            for k, n in enumerate(["K1_p", "K2_spmv_v", "K3_s", "K4_spmv_t", "K5_xr", "init"])},
+                             "peak_kind": peak_kind,
+                             "traffic": None if traffic is None else traffic * loop_rows / max(loop_launches, 1),
+                             "traffic_bytes_per_row_iteration": traffic,
+                             "bytes_per_row_iteration": LOOP_BYTES_PER_ROW,
+                             "fp64_tflops": fp64_tflops, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
+                             "fp64_frac": fp64_tflops / FP64_PEAK_TFLOPS,
+                             "avg_launch_ms": loop_ms / max(loop_launches, 1),
+                             "row_iterations_per_launch": loop_rows / max(loop_launches, 1)},
+                "kernels": dict({n: {"iterations": tot["launches"][k], "ms": round(tot["ms"][k], 3)}
+                                 for k, n in enumerate(["K1_p", "K2_spmv_v", "K3_s", "K4_spmv_t", "K5_xr"])},
+                                k_kr_loop={"launches": loop_launches, "ms": round(loop_ms, 3)}),
                 "gpu_launches": gpu_launches,
                 "krylov_rows": kr_rows,
                 "cpu_baseline": cpu,

@@ -232,9 +232,14 @@ NS3D_API int ns3d_close(ns3d_handle *h);
 /* per-kernel device time of the pressure(-correction) BiCGSTAB kernels,
  * collected with CUDA events on the solver's stream while enabled */
 typedef struct ns3d_profile {
-    int64_t launches[6];      /* K1 p-update, K2 SpMV+dot, K3 s-update, K4 SpMV+dots, K5 x/r-update, init */
-    double ms[6];             /* summed device milliseconds per kernel */
-    int64_t rows[6];          /* summed rows processed (active systems only) */
+    /* index 0-4: the phases of a BiCGSTAB iteration inside the loop kernel
+     * (K1 p-update, K2 SpMV+dot, K3 s-update, K4 SpMV+dots, K5 x/r-update):
+     * launches = iterations, ms = time between the grid barriers that end the
+     * phases (global timer of block 0).  index 5: launches of the loop kernel,
+     * ms by CUDA events.  rows: row-iterations of active systems. */
+    int64_t launches[6];
+    double ms[6];
+    int64_t rows[6];
     int64_t total_launches;   /* every kernel launched by this handle */
 } ns3d_profile;
 NS3D_API int ns3d_set_profiling(ns3d_handle *h, int32_t enable);
@@ -250,7 +255,7 @@ NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
  * multiple of 1024 and >= n), the right-hand side and the guess/solution x
  * (npad doubles each) and a CUDA stream (NULL = default stream).  Work vectors
  * live in a fixed device array inside the library: at most 65536 rows
- * (larger n returns NS3D_ERR_ARG); the array (about 4.6 MiB) is held on every
+ * (larger n returns NS3D_ERR_ARG); the array (about 4.5 MiB) is held on every
  * GPU that loads the library until exit.  The first call on a device looks
  * up the array's device address (cudaGetSymbolAddress), so make it before any
  * stream capture.  All calls share the array: calls that overlap on the GPU

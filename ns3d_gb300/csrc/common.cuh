@@ -35,32 +35,36 @@ __device__ __forceinline__ double warp_tree_sum(double v) {
     return v;
 }
 
-// Block of exactly LANES threads; returns the tree sum in thread 0 (other
-// threads get an unspecified value).  `sm` needs LANES doubles.
-__device__ __forceinline__ double block_tree_sum(double v, double *sm) {
-    const int t = threadIdx.x;
+// Tree sum over LANES threads (lane = this thread's index among them) that
+// synchronize with `sync`: the block's __syncthreads when a block has exactly
+// LANES threads, a named barrier when a larger block holds several groups of
+// LANES threads.  Returns the tree sum in lane 0 (other lanes get an
+// unspecified value).  `sm` needs LANES doubles.
+template <class Sync>
+__device__ __forceinline__ double lanes_tree_sum(double v, int lane, double *sm, Sync sync) {
     v = warp_tree_sum(v);
-    if ((t & 31) == 0) sm[t >> 5] = v;
-    __syncthreads();
+    if ((lane & 31) == 0) sm[lane >> 5] = v;
+    sync();
     double r = 0.0;
-    if (t < 32) {
-        r = (t < LANES / 32) ? sm[t] : 0.0;
+    if (lane < 32) {
+        r = (lane < LANES / 32) ? sm[lane] : 0.0;
         for (int off = LANES / 64; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
     }
-    __syncthreads();
+    sync();
     return r;
 }
 
-// Two tree sums at once, each with exactly the pairings of block_tree_sum.
+// Two tree sums at once, each with exactly the pairings of lanes_tree_sum.
 // After the first level of a warp, lanes 0-15 carry the first sum and lanes
 // 16-31 the second, so every later level is one shuffle and one add for
-// both (FP64 issue is scarce on this GPU).  Results valid in thread 0.
-__device__ __forceinline__ void block_tree_sum2(double a, double b, double *sm, double &ra, double &rb) {
+// both (FP64 issue is scarce on this GPU).  Results valid in lane 0.
+template <class Sync>
+__device__ __forceinline__ void lanes_tree_sum2(double a, double b, int lane, double *sm, double &ra, double &rb,
+                                                Sync sync) {
     static_assert(2 * (LANES / 32) <= 32, "warp sums of both trees fit one warp");
-    const int t = threadIdx.x;
     ra = 0.0;
     rb = 0.0;
-    const bool lo = (t & 16) == 0;
+    const bool lo = (lane & 16) == 0;
     // offset 16: lane l < 16 forms a_l + a_(l+16), lane l >= 16 forms b_(l-16) + b_l
     double v = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
     v = v + __shfl_down_sync(0xffffffffu, v, 8);
@@ -68,17 +72,36 @@ __device__ __forceinline__ void block_tree_sum2(double a, double b, double *sm, 
     v = v + __shfl_down_sync(0xffffffffu, v, 2);
     v = v + __shfl_down_sync(0xffffffffu, v, 1);
     constexpr int NW = LANES / 32;
-    if ((t & 31) == 0) sm[t >> 5] = v;
-    if ((t & 31) == 16) sm[NW + (t >> 5)] = v;
-    __syncthreads();
-    if (t < 32) {
-        double r = (t < 2 * NW) ? sm[t] : 0.0;
+    if ((lane & 31) == 0) sm[lane >> 5] = v;
+    if ((lane & 31) == 16) sm[NW + (lane >> 5)] = v;
+    sync();
+    if (lane < 32) {
+        double r = (lane < 2 * NW) ? sm[lane] : 0.0;
         for (int off = NW / 2; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
         const double r2 = __shfl_sync(0xffffffffu, r, NW);
         ra = r;
         rb = r2;
     }
-    __syncthreads();
+    sync();
+}
+
+struct BlockSync {
+    __device__ __forceinline__ void operator()() const { __syncthreads(); }
+};
+// named barrier `id` (1..15) over the LANES threads of one group
+struct GroupSync {
+    int id;
+    __device__ __forceinline__ void operator()() const {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "n"(LANES) : "memory");
+    }
+};
+
+// Block of exactly LANES threads; the tree sum in thread 0.
+__device__ __forceinline__ double block_tree_sum(double v, double *sm) {
+    return lanes_tree_sum(v, threadIdx.x, sm, BlockSync());
+}
+__device__ __forceinline__ void block_tree_sum2(double a, double b, double *sm, double &ra, double &rb) {
+    lanes_tree_sum2(a, b, threadIdx.x, sm, ra, rb, BlockSync());
 }
 
 __device__ __forceinline__ double dmaxv(double a, double b) { return (b > a) ? b : a; }
@@ -104,22 +127,32 @@ __device__ __forceinline__ double block_tree_min(double v, double *sm) { return 
 
 // Final combination of `n` chunk partials (strided by `stride` doubles):
 // lane l sums partials l, l+LANES, ... in order, then the halving tree.
-// Result valid in thread 0.
-__device__ __forceinline__ double final_partials_sum(const double *part, int n, int stride, double *sm) {
+// Result valid in lane 0.
+template <class Sync>
+__device__ __forceinline__ double lanes_final_sum(const double *part, int n, int stride, int lane, double *sm,
+                                                  Sync sync) {
     double a = 0.0;
-    for (int i = threadIdx.x; i < n; i += LANES) a = a + __ldcg(part + (size_t)i * stride);
-    return block_tree_sum(a, sm);
+    for (int i = lane; i < n; i += LANES) a = a + __ldcg(part + (size_t)i * stride);
+    return lanes_tree_sum(a, lane, sm, sync);
 }
-
-// final_partials_sum of the interleaved pairs part[2i] and part[2i+1]
-__device__ __forceinline__ void final_partials_sum2(const double *part, int n, double *sm, double &ra, double &rb) {
+// the same for the interleaved pairs part[2i] and part[2i+1] (16-byte aligned)
+template <class Sync>
+__device__ __forceinline__ void lanes_final_sum2(const double *part, int n, int lane, double *sm, double &ra,
+                                                 double &rb, Sync sync) {
     double a = 0.0, b = 0.0;
-    for (int i = threadIdx.x; i < n; i += LANES) {
+    for (int i = lane; i < n; i += LANES) {
         const double2 q = __ldcg(reinterpret_cast<const double2 *>(part) + i);
         a = a + q.x;
         b = b + q.y;
     }
-    block_tree_sum2(a, b, sm, ra, rb);
+    lanes_tree_sum2(a, b, lane, sm, ra, rb, sync);
+}
+
+__device__ __forceinline__ double final_partials_sum(const double *part, int n, int stride, double *sm) {
+    return lanes_final_sum(part, n, stride, threadIdx.x, sm, BlockSync());
+}
+__device__ __forceinline__ void final_partials_sum2(const double *part, int n, double *sm, double &ra, double &rb) {
+    lanes_final_sum2(part, n, threadIdx.x, sm, ra, rb, BlockSync());
 }
 
 inline int ceil_div(long a, long b) { return (int)((a + b - 1) / b); }

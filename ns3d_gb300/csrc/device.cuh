@@ -113,7 +113,7 @@ struct KSys {  // one system of a solve set (device array)
     const double *invdiag;
     const double *b;
     double *x, *r, *r0, *p, *v, *y, *s, *z, *t;
-    double *part;  // [nchunks][2]
+    double *part;  // [5 * nchunks]: reduction partials (layout in krylov.cu)
     KState *st;
 };
 
@@ -123,6 +123,21 @@ constexpr int KMAX = 4;
 struct KSetArg {
     int nsys, total_chunks;
     KSys sys[KMAX];
+};
+
+// The persistent BiCGSTAB loop kernel: block shape and its grid barrier.
+constexpr int LOOP_THREADS = 1024;
+constexpr int LOOP_GROUPS = LOOP_THREADS / LANES;
+struct GridBar {  // counter, generation and error flag on separate 128-byte lines
+    unsigned int count, pad0_[31];
+    unsigned int gen, pad1_[31];
+    int err, pad2_[31];
+};
+// per-phase time of the loop kernel (block 0, ns of the global timer)
+struct LoopProf {
+    unsigned long long ns[5];
+    long long iters;
+    int ok, pad_;
 };
 
 }  // namespace ns3d

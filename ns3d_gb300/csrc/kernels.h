@@ -11,6 +11,8 @@ struct Grid;
 struct SysView;
 struct KSys;
 struct KSetArg;
+struct GridBar;
+struct LoopProf;
 struct KState;
 
 // geometry.cu
@@ -73,12 +75,11 @@ void launch_face_average(const Grid &g, const double *u, const double *v, const 
 
 // krylov.cu: batched BiCGSTAB over a set of systems
 void launch_krylov_init(const KSetArg &set, cudaStream_t st);
-void launch_krylov_iteration(const KSetArg &set, cudaStream_t st);
+// iterations until every system is done, one needs a restart, or max_iters
+cudaError_t launch_krylov_loop(const KSetArg &set, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st);
 void launch_krylov_restart(const KSetArg &set, cudaStream_t st);
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st);
 int device_sm_count();
-// K1..K5 of one BiCGSTAB iteration launched one at a time (profiling)
-void launch_krylov_kernel(int which, const KSetArg &set, cudaStream_t st);
 // kernels launched by this library since it was loaded
 int64_t launch_count();
 void count_launches(int64_t n);

@@ -220,133 +220,221 @@ __global__ void k_kr_init2(const __grid_constant__ KSetArg A) {
     }
 }
 
-// K1: p = r + beta (p - w v); y = D^-1 p
-__global__ void __launch_bounds__(LANES) k_kr_p(const __grid_constant__ KSetArg A) {
-    NS3D_CHUNK_LOOP
-        if (!sys_active(S)) continue;
-        const double beta = __ldcg(&S.st->beta), w = __ldcg(&S.st->w);
-        const Row4 r = ld4(S.r + r0), v = ld4(S.v + r0), iv = ld4(S.invdiag + r0);
-        Row4 p = ld4(S.p + r0), y;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            p.v[m] = __fma_rn(beta, __fma_rn(-w, v.v[m], p.v[m]), r.v[m]);
-            y.v[m] = iv.v[m] * p.v[m];
-        }
-        st4(S.p + r0, p);
-        st4(S.y + r0, y);
-    }
+// ---- the BiCGSTAB iteration loop: one persistent cooperative kernel ----------
+//
+// LOOP_THREADS threads per block form LOOP_GROUPS groups of LANES threads; a
+// group processes whole chunks (its lanes own the rows of the fixed
+// reduction order) and reduces them with a named barrier.  Every block keeps
+// a copy of the per-system scalars in shared memory; after each grid-wide
+// barrier every block combines the chunk partials of each system in the
+// fixed order itself (group s for system s), so all copies stay bit-identical
+// without a broadcast.  Partials of the three reductions of an iteration go
+// to separate regions of S.part, so a block that runs ahead never overwrites
+// partials another block is still combining:
+//   [0, 2n)  <t,t>, <t,s> pairs     [2n, 4n)  <r0,r>, <r,r> pairs
+//   [4n, 5n) <r0,v>
+// The loop ends when every system is done, when a system needs a restart
+// (the host recomputes its residual and launches the loop again), after
+// `max_iters` iterations, or when a grid barrier gives up waiting.
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
 }
 
-// K2: v = A y, <r0, v> -> alpha = rho / <r0, v>
-__global__ void __launch_bounds__(LANES) k_kr_v(const __grid_constant__ KSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[2];
-    NS3D_CHUNK_LOOP
-        if (!sys_active(S)) continue;
-        const Row4 v = spmv4(S, r0, S.y);
-        const Row4 rr0 = ld4(S.r0 + r0);
-        double a = 0.0;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m)
-            if (r0 + m * LANES < S.n) a = __fma_rn(rr0.v[m], v.v[m], a);
-        st4(S.v + r0, v);
-        const double t = block_tree_sum(a, sm);
-        if (threadIdx.x == 0) S.part[2 * (size_t)lc] = t;
-        if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
-            const double d = final_partials_sum(S.part, S.nchunks, 2, sm);
-            if (threadIdx.x == 0) {
-                S.st->counter = 0;
-                S.st->alpha = S.st->rho / d;
+// Grid-wide barrier of a cooperative launch.  Thread 0 of each block
+// arrives on the counter; the last to arrive resets it and advances the
+// generation, the others wait for the generation to move.  The wait gives
+// up after kBarrierLimitNs (or 2^31 polls): the block records the failure in
+// bar->err and returns false, and the kernel stops at once -- so a launch
+// always terminates, and the host reports the error.
+constexpr unsigned long long kBarrierLimitNs = 4000000000ull;
+
+__device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &gen, int *s_ok) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        __threadfence();
+        const unsigned int prev = atomicAdd(&bar->count, 1u);
+        if (prev == gridDim.x - 1) {
+            atomicExch(&bar->count, 0u);
+            __threadfence();
+            atomicAdd(&bar->gen, 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            unsigned int polls = 0;
+            while (*(volatile unsigned int *)&bar->gen == gen) {
+                if ((++polls & 255u) == 0 && (global_ns() - t0 > kBarrierLimitNs || polls > 0x7fffffffu)) {
+                    atomicExch(&bar->err, 1);
+                    ok = 0;
+                    break;
+                }
             }
         }
+        __threadfence();
+        gen += 1;
+        *s_ok = ok;
     }
+    __syncthreads();
+    return *s_ok != 0;
 }
 
-// K3: s = r - alpha v; z = D^-1 s
-__global__ void __launch_bounds__(LANES) k_kr_s(const __grid_constant__ KSetArg A) {
-    NS3D_CHUNK_LOOP
-        if (!sys_active(S)) continue;
-        const double alpha = __ldcg(&S.st->alpha);
-        const Row4 r = ld4(S.r + r0), v = ld4(S.v + r0), iv = ld4(S.invdiag + r0);
-        Row4 s, z;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            s.v[m] = __fma_rn(-alpha, v.v[m], r.v[m]);
-            z.v[m] = iv.v[m] * s.v[m];
+__device__ __forceinline__ bool state_active(const KState &k) { return (k.done | k.paused) == 0; }
+
+__global__ void __launch_bounds__(LOOP_THREADS, 1)
+    k_kr_loop(const __grid_constant__ KSetArg A, GridBar *bar, LoopProf *prof, int max_iters) {
+    __shared__ KState sst[KMAX];
+    __shared__ double sm[LOOP_GROUPS][LANES];
+    __shared__ int s_ok;
+    const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
+    const GroupSync gsync{gi + 1};
+    const int gstride = gridDim.x * LOOP_GROUPS;
+    const int cbegin = blockIdx.x * LOOP_GROUPS + gi;
+    if (threadIdx.x < A.nsys) sst[threadIdx.x] = *A.sys[threadIdx.x].st;
+    unsigned int gen = 0;
+    if (threadIdx.x == 0) gen = *(volatile unsigned int *)&bar->gen;
+    __syncthreads();
+    // phase times of block 0 (thread 0), kept in shared memory
+    __shared__ unsigned long long s_tp[6];
+    const bool timing = prof != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
+    if (timing) {
+        for (int k = 0; k < 5; ++k) s_tp[k] = 0;
+        s_tp[5] = global_ns();
+    }
+    auto mark = [&](int k) {
+        if (timing) {
+            const unsigned long long t = global_ns();
+            s_tp[k] += t - s_tp[5];
+            s_tp[5] = t;
         }
-        st4(S.s + r0, s);
-        st4(S.z + r0, z);
-    }
-}
-
-// K4: t = A z, <t, t>, <t, s> -> w
-__global__ void __launch_bounds__(LANES) k_kr_t(const __grid_constant__ KSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[2];
-    NS3D_CHUNK_LOOP
-        if (!sys_active(S)) continue;
-        const Row4 t = spmv4(S, r0, S.z);
-        const Row4 s = ld4(S.s + r0);
-        double att = 0.0, ats = 0.0;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m)
-            if (r0 + m * LANES < S.n) {
-                att = __fma_rn(t.v[m], t.v[m], att);
-                ats = __fma_rn(t.v[m], s.v[m], ats);
+    };
+    int it = 0;
+    bool ok = true;
+    for (; it < max_iters; ++it) {
+        // K1: p = r + beta (p - w v); y = D^-1 p
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = sys_of_chunk(A, c);
+            if (!state_active(sst[si])) continue;
+            const KSys &S = A.sys[si];
+            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const double beta = sst[si].beta, w = sst[si].w;
+#pragma unroll 4
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const double p = __fma_rn(beta, __fma_rn(-w, S.v[row], S.p[row]), S.r[row]);
+                S.p[row] = p;
+                S.y[row] = S.invdiag[row] * p;
             }
-        st4(S.t + r0, t);
-        double tt, ts;
-        block_tree_sum2(att, ats, sm, tt, ts);
-        if (threadIdx.x == 0) {
-            S.part[2 * (size_t)lc + 0] = tt;
-            S.part[2 * (size_t)lc + 1] = ts;
         }
-        if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
+        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        mark(0);
+        // K2: v = A y, <r0, v>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = sys_of_chunk(A, c);
+            if (!state_active(sst[si])) continue;
+            const KSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            double a = 0.0;
+#pragma unroll 2
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const double v = spmv_row(S, row, S.y);
+                S.v[row] = v;
+                if (row < S.n) a = __fma_rn(S.r0[row], v, a);
+            }
+            const double t = lanes_tree_sum(a, lane, sm[gi], gsync);
+            if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
+        }
+        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (gi < A.nsys && state_active(sst[gi])) {
+            const KSys &S = A.sys[gi];
+            const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks, S.nchunks, 1, lane, sm[gi], gsync);
+            if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+        }
+        __syncthreads();
+        mark(1);
+        // K3: s = r - alpha v; z = D^-1 s
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = sys_of_chunk(A, c);
+            if (!state_active(sst[si])) continue;
+            const KSys &S = A.sys[si];
+            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const double alpha = sst[si].alpha;
+#pragma unroll 4
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const double sv = __fma_rn(-alpha, S.v[row], S.r[row]);
+                S.s[row] = sv;
+                S.z[row] = S.invdiag[row] * sv;
+            }
+        }
+        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        mark(2);
+        // K4: t = A z, <t, t>, <t, s>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = sys_of_chunk(A, c);
+            if (!state_active(sst[si])) continue;
+            const KSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            double att = 0.0, ats = 0.0;
+#pragma unroll 2
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const double t = spmv_row(S, row, S.z);
+                S.t[row] = t;
+                if (row < S.n) {
+                    att = __fma_rn(t, t, att);
+                    ats = __fma_rn(t, S.s[row], ats);
+                }
+            }
+            double tt, ts;
+            lanes_tree_sum2(att, ats, lane, sm[gi], tt, ts, gsync);
+            if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
+        }
+        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (gi < A.nsys && state_active(sst[gi])) {
+            const KSys &S = A.sys[gi];
             double ftt, fts;
-            final_partials_sum2(S.part, S.nchunks, sm, ftt, fts);
-            if (threadIdx.x == 0) {
-                S.st->counter = 0;
-                S.st->w = (ftt > 0.0) ? fts / ftt : 0.0;
+            lanes_final_sum2(S.part, S.nchunks, lane, sm[gi], ftt, fts, gsync);
+            if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+        }
+        __syncthreads();
+        mark(3);
+        // K5: x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = sys_of_chunk(A, c);
+            if (!state_active(sst[si])) continue;
+            const KSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            const double alpha = sst[si].alpha, w = sst[si].w;
+            double a0r = 0.0, arr = 0.0;
+#pragma unroll 4
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                // rows >= n of x are padding; they receive values computed from zeros
+                S.x[row] = __fma_rn(w, S.z[row], __fma_rn(alpha, S.y[row], S.x[row]));
+                const double r = __fma_rn(-w, S.t[row], S.s[row]);
+                S.r[row] = r;
+                if (row < S.n) {
+                    a0r = __fma_rn(S.r0[row], r, a0r);
+                    arr = __fma_rn(r, r, arr);
+                }
             }
+            double t0r, trr;
+            lanes_tree_sum2(a0r, arr, lane, sm[gi], t0r, trr, gsync);
+            if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks)[lc] = make_double2(t0r, trr);
         }
-    }
-}
-
-// K5: x += alpha y + w z; r = s - w t; <r0, r>, <r, r> -> loop control
-__global__ void __launch_bounds__(LANES) k_kr_x(const __grid_constant__ KSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[2];
-    NS3D_CHUNK_LOOP
-        if (!sys_active(S)) continue;
-        const double alpha = __ldcg(&S.st->alpha), w = __ldcg(&S.st->w);
-        const Row4 y = ld4(S.y + r0), z = ld4(S.z + r0), t = ld4(S.t + r0), s = ld4(S.s + r0);
-        const Row4 rr0 = ld4(S.r0 + r0);
-        Row4 x = ld4(S.x + r0), r;
-        double a0r = 0.0, arr = 0.0;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            x.v[m] = __fma_rn(w, z.v[m], __fma_rn(alpha, y.v[m], x.v[m]));
-            r.v[m] = __fma_rn(-w, t.v[m], s.v[m]);
-            if (r0 + m * LANES < S.n) {
-                a0r = __fma_rn(rr0.v[m], r.v[m], a0r);
-                arr = __fma_rn(r.v[m], r.v[m], arr);
-            }
-        }
-        // rows >= n of x are padding; they receive values computed from zeros
-        st4(S.x + r0, x);
-        st4(S.r + r0, r);
-        double t0r, trr;
-        block_tree_sum2(a0r, arr, sm, t0r, trr);
-        if (threadIdx.x == 0) {
-            S.part[2 * (size_t)lc + 0] = t0r;
-            S.part[2 * (size_t)lc + 1] = trr;
-        }
-        if (arrive_last(S.st, (unsigned)S.nchunks, sh)) {
+        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (gi < A.nsys && state_active(sst[gi])) {
+            const KSys &S = A.sys[gi];
             double f0r, frr;
-            final_partials_sum2(S.part, S.nchunks, sm, f0r, frr);
-            if (threadIdx.x == 0) {
-                KState *st = S.st;
-                st->counter = 0;
+            lanes_final_sum2(S.part + 2 * (size_t)S.nchunks, S.nchunks, lane, sm[gi], f0r, frr, gsync);
+            if (lane == 0) {
+                KState *st = &sst[gi];
                 st->rr = frr;
                 st->iter += 1;
                 st->work += 1;
@@ -355,7 +443,7 @@ __global__ void __launch_bounds__(LANES) k_kr_x(const __grid_constant__ KSetArg 
                 } else {
                     const double eps2 = DBL_EPSILON * DBL_EPSILON;
                     if (fabs(f0r) < eps2 * st->r0_sqnorm) {
-                        st->paused = 1;  // host recomputes r = b - A x and r0
+                        st->paused = 1;  // the host recomputes r = b - A x and r0
                     } else {
                         st->beta = (f0r / st->rho) * (st->alpha / st->w);
                         st->rho = f0r;
@@ -363,6 +451,27 @@ __global__ void __launch_bounds__(LANES) k_kr_x(const __grid_constant__ KSetArg 
                 }
             }
         }
+        __syncthreads();
+        mark(4);
+        bool any_active = false, any_paused = false;
+        for (int q = 0; q < A.nsys; ++q) {
+            any_active = any_active || state_active(sst[q]);
+            any_paused = any_paused || (sst[q].paused != 0 && sst[q].done == 0);
+        }
+        if (!any_active || any_paused) {
+            ++it;
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < A.nsys) {
+        KState k = sst[threadIdx.x];
+        k.counter = 0;
+        *A.sys[threadIdx.x].st = k;
+    }
+    if (timing) {
+        for (int k = 0; k < 5; ++k) prof->ns[k] += s_tp[k];
+        prof->iters += it;
+        prof->ok = ok ? 1 : 0;
     }
 }
 
@@ -441,28 +550,27 @@ void launch_krylov_init(const KSetArg &A, cudaStream_t st) {
     k_kr_init2<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
-void launch_krylov_iteration(const KSetArg &A, cudaStream_t st) {
-    if (A.total_chunks <= 0) return;
-    const int g = kr_grid(A.total_chunks);
-    count_launches(5);
-    k_kr_p<<<g, LANES, 0, st>>>(A);
-    k_kr_v<<<g, LANES, 0, st>>>(A);
-    k_kr_s<<<g, LANES, 0, st>>>(A);
-    k_kr_t<<<g, LANES, 0, st>>>(A);
-    k_kr_x<<<g, LANES, 0, st>>>(A);
-}
+static std::atomic<int> g_loop_occ{0};
 
-void launch_krylov_kernel(int which, const KSetArg &A, cudaStream_t st) {
-    if (A.total_chunks <= 0) return;
-    const int g = kr_grid(A.total_chunks);
-    count_launches(1);
-    switch (which) {
-        case 0: k_kr_p<<<g, LANES, 0, st>>>(A); break;
-        case 1: k_kr_v<<<g, LANES, 0, st>>>(A); break;
-        case 2: k_kr_s<<<g, LANES, 0, st>>>(A); break;
-        case 3: k_kr_t<<<g, LANES, 0, st>>>(A); break;
-        default: k_kr_x<<<g, LANES, 0, st>>>(A); break;
+cudaError_t launch_krylov_loop(const KSetArg &A, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st) {
+    if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
+    int occ = g_loop_occ.load();
+    if (occ == 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kr_loop, LOOP_THREADS, 0);
+        if (e != cudaSuccess) return e;
+        if (occ <= 0) return cudaErrorLaunchOutOfResources;
+        g_loop_occ = occ;
     }
+    // every block must be resident at once (cooperative launch); small sets
+    // use fewer blocks so that concurrent solves can share the GPU
+    const int need = (A.total_chunks + LOOP_GROUPS - 1) / LOOP_GROUPS;
+    const int grid = std::max(1, std::min(need, device_sm_count() * occ));
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
+    if (e != cudaSuccess) return e;
+    KSetArg a = A;
+    void *args[] = {&a, &bar, &prof, &max_iters};
+    count_launches(1);
+    return cudaLaunchCooperativeKernel((const void *)k_kr_loop, grid, LOOP_THREADS, args, 0, st);
 }
 
 void launch_krylov_restart(const KSetArg &A, cudaStream_t st) {

@@ -6,9 +6,10 @@
 // allocation, and embedded/real-time hosts that forbid allocation after
 // initialisation.  ns3d_bicgstab_noalloc serves them: the caller passes the
 // system (device pointers) and the vectors; every work vector, the chunk
-// partials and the solver state live in one file-scope device array of fixed
-// size, kScratchRows rows (65536), declared below.  Every GPU that loads the
-// library holds that array (about 4.6 MiB) until the process exits.
+// partials, the solver state and the loop kernel's grid barrier live in one
+// file-scope device array of fixed size, kScratchRows rows (65536), declared
+// below.  Every GPU that loads the
+// library holds that array (about 4.5 MiB) until the process exits.
 //
 // Host code cannot use the array's name as a device address (it names a
 // host-side stand-in), so the first call on each device looks the address up
@@ -30,10 +31,11 @@ constexpr int kScratchRows = 1 << 16;
 constexpr int kScratchChunks = kScratchRows / CH;
 constexpr int kVectors = 9;  // r, r0, p, v, y, s, z, t, invdiag
 constexpr size_t kVecBytes = (size_t)kVectors * kScratchRows * sizeof(double);
-constexpr size_t kPartBytes = (size_t)2 * kScratchChunks * sizeof(double);
+constexpr size_t kPartBytes = (size_t)5 * kScratchChunks * sizeof(double);
 constexpr size_t kStateOffset = kVecBytes + kPartBytes;
-constexpr size_t kScratchBytes = kStateOffset + 256;
-static_assert(sizeof(KState) <= 256, "scratch layout");
+constexpr size_t kBarOffset = kStateOffset + 256;
+constexpr size_t kScratchBytes = kBarOffset + 512;
+static_assert(sizeof(KState) <= 256 && sizeof(GridBar) <= 512, "scratch layout");
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -99,6 +101,7 @@ extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t 
     double *vec = (double *)base;
     double *part = (double *)(base + kVecBytes);
     KState *dst = (KState *)(base + kStateOffset);
+    GridBar *bar = (GridBar *)(base + kBarOffset);
     const int nchunks = (n + CH - 1) / CH;
 
     KSetArg set;
@@ -137,17 +140,25 @@ extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t 
     launch_krylov_init(set, st);
     const long cap = 2L * maxit + 64;
     long issued = 0;
-    int batch = 4;
+    int work_before = 0, bar_err = 0;
+    bool launched = false;
     KState h;
     while (true) {
-        if (!ok(cudaMemcpyAsync(&h, dst, sizeof h, cudaMemcpyDeviceToHost, st)) || !ok(cudaStreamSynchronize(st)))
+        if (!ok(cudaMemcpyAsync(&h, dst, sizeof h, cudaMemcpyDeviceToHost, st)) ||
+            !ok(cudaMemcpyAsync(&bar_err, &bar->err, sizeof bar_err, cudaMemcpyDeviceToHost, st)) ||
+            !ok(cudaStreamSynchronize(st)))
             return fail(NS3D_ERR_CUDA, "CUDA error while solving (see cudaGetLastError)");
+        if (launched && bar_err) return fail(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel: a grid barrier timed out");
         if (h.done) break;
+        if (launched && h.work == work_before && !h.paused)
+            return fail(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel made no progress");
+        issued += h.work - work_before;
+        work_before = h.work;
         if (issued >= cap) return fail(NS3D_ERR_TIMEOUT, "BiCGSTAB exceeded its iteration bound");
         if (h.paused) launch_krylov_restart(set, st);
-        for (int b = 0; b < batch; ++b) launch_krylov_iteration(set, st);
-        issued += batch;
-        batch = std::min(64, batch * 2);
+        if (!ok(launch_krylov_loop(set, bar, nullptr, (int)(cap - issued), st)))
+            return fail(NS3D_ERR_CUDA, "cooperative launch of the BiCGSTAB loop kernel failed");
+        launched = true;
     }
     info->iterations = h.iter;
     info->info = h.info;

@@ -131,7 +131,9 @@ class KrylovSet {
     long launches() const { return launches_; }
     void reset_launch_count() { launches_ = 0; }
 
-    // per-kernel CUDA-event timing of K1..K5 (index 0..4) and init (5)
+    // timing of the loop kernel: phases K1..K5 (index 0..4, block 0's view
+    // between grid barriers, global timer) and whole launches (index 5,
+    // CUDA events); rows = row-iterations
     struct Profile {
         int64_t launches[6] = {0, 0, 0, 0, 0, 0};
         double ms[6] = {0, 0, 0, 0, 0, 0};
@@ -143,12 +145,13 @@ class KrylovSet {
 
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
-    void issue_batch(int batch, cudaStream_t st);
-    void collect_batch(int batch, const std::vector<int> &work_before);
-    std::vector<cudaEvent_t> events_;
+    cudaEvent_t ev_[2] = {nullptr, nullptr};
     KSetArg set_;  // passed to every kernel by value
     DBuf<KState> st_;
     HBuf<KState> h_st_, h_up_;
+    DBuf<GridBar> bar_;
+    DBuf<LoopProf> prof_;
+    HBuf<int> h_err_;
     int nsys_ = 0, total_chunks_ = 0;
     int prev_iters_ = 8;
     long launches_ = 0;

@@ -40,7 +40,7 @@ void DevSys::allocate(int rows, int first_extent, cudaStream_t st) {
     invdiag.alloc_zero(npad, st);
     DBuf<double> *ws[] = {&r, &r0, &p, &v, &y, &s, &z, &t};
     for (auto *b : ws) b->alloc_zero(npad, st);
-    part.alloc_zero((size_t)2 * std::max(nchunks, 1), st);
+    part.alloc_zero((size_t)5 * std::max(nchunks, 1), st);
 }
 
 size_t DevSys::device_bytes() const {
@@ -77,6 +77,12 @@ void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) 
         h_st_.alloc(ns);
         h_up_.alloc(ns);
     }
+    if (!bar_.n) {
+        bar_.alloc_zero(1, st);
+        prof_.alloc_zero(1, st);
+        h_err_.alloc(1);
+        for (cudaEvent_t &e : ev_) NS3D_CUDA_CHECK(cudaEventCreate(&e));
+    }
     std::memset(&set_, 0, sizeof set_);
     set_.nsys = ns;
     set_.total_chunks = chunk;
@@ -110,35 +116,63 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
     NS3D_CUDA_CHECK(cudaMemcpyAsync(st_.p, h_up_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
     launch_krylov_init(set_, st);
     launches_ += 2;
-    // Iterations are issued in batches; finished systems make the kernels
-    // return at once, so a batch may overshoot the last iteration harmlessly.
-    // Restarts reset the iteration counter once, so 2*maxit bounds the loop.
+    if (profiling) NS3D_CUDA_CHECK(cudaMemsetAsync(prof_.p, 0, sizeof(LoopProf), st));
+    // The loop kernel runs until every system is done or one needs a
+    // restart; restarts reset the iteration counter once, so 2*maxit+64
+    // iterations bound the whole solve.
     const long cap = 2L * maxit + 64;
     long issued = 0;
-    int batch = std::max(1, std::min(32, prev_iters_ / 2));
-    int max_iters = 0, last_batch = 0;
+    int max_iters = 0, loops = 0;
     std::vector<int> work_before(ns, 0);
     while (true) {
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(h_err_.p, &bar_.p->err, sizeof(int), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
-        if (profiling && last_batch > 0) collect_batch(last_batch, work_before);
+        if (h_err_.p[0]) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel: a grid barrier timed out");
         bool all_done = true, any_paused = false;
+        int progress = 0;
+        int64_t rows = 0;
         for (int i = 0; i < ns; ++i) {
-            if (!h_st_.p[i].done) all_done = false;
-            if (h_st_.p[i].paused && !h_st_.p[i].done) any_paused = true;
-            work_before[i] = h_st_.p[i].work;
+            const KState &k = h_st_.p[i];
+            if (!k.done) all_done = false;
+            if (k.paused && !k.done) any_paused = true;
+            if (loops > 0) {
+                progress = std::max(progress, k.work - work_before[i]);
+                rows += (int64_t)set_.sys[i].n * (k.work - work_before[i]);
+            }
+            work_before[i] = k.work;
         }
+        if (profiling && loops > 0) {
+            float ms = 0;
+            NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+            prof.launches[5] += 1;
+            prof.ms[5] += ms;
+            prof.rows[5] += rows;
+            for (int k = 0; k < 5; ++k) prof.rows[k] += rows;
+        }
+        issued += progress;
         if (all_done) break;
+        if (loops > 0 && progress == 0 && !any_paused)
+            throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel made no progress");
         if (issued >= cap) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB driver exceeded its iteration bound");
         if (any_paused) {
             launch_krylov_restart(set_, st);
             launches_ += 1;
         }
-        issue_batch(batch, st);
-        last_batch = batch;
-        launches_ += 5L * batch;
-        issued += batch;
-        batch = std::min(64, batch * 2);
+        if (profiling) NS3D_CUDA_CHECK(cudaEventRecord(ev_[0], st));
+        NS3D_CUDA_CHECK(launch_krylov_loop(set_, bar_.p, profiling ? prof_.p : nullptr, (int)(cap - issued), st));
+        if (profiling) NS3D_CUDA_CHECK(cudaEventRecord(ev_[1], st));
+        launches_ += 1;
+        loops += 1;
+    }
+    if (profiling) {
+        LoopProf lp;
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(&lp, prof_.p, sizeof lp, cudaMemcpyDeviceToHost, st));
+        NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+        for (int k = 0; k < 5; ++k) {
+            prof.ms[k] += 1e-6 * (double)lp.ns[k];
+            prof.launches[k] += lp.iters;
+        }
     }
     for (int i = 0; i < ns; ++i) {
         const KState &k = h_st_.p[i];
@@ -153,41 +187,8 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
 }
 
 KrylovSet::~KrylovSet() {
-    for (cudaEvent_t e : events_) cudaEventDestroy(e);
-}
-
-void KrylovSet::issue_batch(int batch, cudaStream_t st) {
-    if (!profiling) {
-        for (int b = 0; b < batch; ++b) launch_krylov_iteration(set_, st);
-        return;
-    }
-    const size_t need = (size_t)batch * 5 + 1;
-    while (events_.size() < need) {
-        cudaEvent_t e;
-        NS3D_CUDA_CHECK(cudaEventCreate(&e));
-        events_.push_back(e);
-    }
-    NS3D_CUDA_CHECK(cudaEventRecord(events_[0], st));
-    for (int b = 0; b < batch; ++b)
-        for (int k = 0; k < 5; ++k) {
-            launch_krylov_kernel(k, set_, st);
-            NS3D_CUDA_CHECK(cudaEventRecord(events_[(size_t)b * 5 + k + 1], st));
-        }
-}
-
-void KrylovSet::collect_batch(int batch, const std::vector<int> &work_before) {
-    for (int b = 0; b < batch; ++b) {
-        int64_t rows = 0;
-        for (int i = 0; i < nsys_; ++i)
-            if (h_st_.p[i].work - work_before[i] > b) rows += set_.sys[i].n;
-        for (int k = 0; k < 5; ++k) {
-            float ms = 0;
-            NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, events_[(size_t)b * 5 + k], events_[(size_t)b * 5 + k + 1]));
-            prof.ms[k] += ms;
-            prof.launches[k] += 1;
-            prof.rows[k] += rows;
-        }
-    }
+    for (cudaEvent_t e : ev_)
+        if (e) cudaEventDestroy(e);
 }
 
 // ============================ solver instance ================================
