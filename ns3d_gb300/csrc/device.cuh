@@ -126,12 +126,14 @@ struct KSetArg {
 };
 
 // The persistent BiCGSTAB loop kernel: block shape and its grid barrier.
-constexpr int LOOP_THREADS = 1024;
+#ifndef NS3D_LOOP_THREADS
+#define NS3D_LOOP_THREADS 1024
+#endif
+constexpr int LOOP_THREADS = NS3D_LOOP_THREADS;
 constexpr int LOOP_GROUPS = LOOP_THREADS / LANES;
-struct GridBar {  // counter, generation and error flag on separate 128-byte lines
+struct GridBar {  // arrival counter and error flag on separate 128-byte lines
     unsigned int count, pad0_[31];
-    unsigned int gen, pad1_[31];
-    int err, pad2_[31];
+    int err, pad1_[31];
 };
 // per-phase time of the loop kernel (block 0, ns of the global timer)
 struct LoopProf {

@@ -243,28 +243,32 @@ __device__ __forceinline__ unsigned long long global_ns() {
     return t;
 }
 
-// Grid-wide barrier of a cooperative launch.  Thread 0 of each block
-// arrives on the counter; the last to arrive resets it and advances the
-// generation, the others wait for the generation to move.  The wait gives
-// up after kBarrierLimitNs (or 2^31 polls): the block records the failure in
-// bar->err and returns false, and the kernel stops at once -- so a launch
-// always terminates, and the host reports the error.
+// Grid-wide barrier of a cooperative launch.  The arrival counter only
+// grows: barrier k of a launch ends when it reaches k * gridDim.x, so a
+// waiting block sees the end as soon as the last arrival lands (no reset, no
+// second flag).  The wait gives up after kBarrierLimitNs (or 2^31 polls):
+// the block records the failure in bar->err and returns false, and the
+// kernel stops at once -- so a launch always terminates, and the host
+// reports the error.
 constexpr unsigned long long kBarrierLimitNs = 4000000000ull;
 
-__device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &gen, int *s_ok) {
+__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
+    unsigned int v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, int *s_ok) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        __threadfence();
-        const unsigned int prev = atomicAdd(&bar->count, 1u);
-        if (prev == gridDim.x - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
+        target += gridDim.x;
+        __threadfence();  // the block's writes (ordered before by the block barrier) become visible
+        atomicAdd(&bar->count, 1u);
+        if ((int)(ld_acquire(&bar->count) - target) < 0) {
             const unsigned long long t0 = global_ns();
             unsigned int polls = 0;
-            while (*(volatile unsigned int *)&bar->gen == gen) {
+            while ((int)(ld_acquire(&bar->count) - target) < 0) {
                 if ((++polls & 255u) == 0 && (global_ns() - t0 > kBarrierLimitNs || polls > 0x7fffffffu)) {
                     atomicExch(&bar->err, 1);
                     ok = 0;
@@ -273,12 +277,17 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &gen, int *
             }
         }
         __threadfence();
-        gen += 1;
         *s_ok = ok;
     }
     __syncthreads();
     return *s_ok != 0;
 }
+
+// rows of a chunk in flight per thread in the SpMV phases (register budget)
+#ifndef NS3D_SPMV_UNROLL
+#define NS3D_SPMV_UNROLL 2
+#endif
+constexpr int kSpmvUnroll = NS3D_SPMV_UNROLL;
 
 __device__ __forceinline__ bool state_active(const KState &k) { return (k.done | k.paused) == 0; }
 
@@ -289,12 +298,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
     __shared__ int s_ok;
     const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
     const GroupSync gsync{gi + 1};
+    // chunk c belongs to block c % gridDim.x (group (c / gridDim.x) % LOOP_GROUPS):
+    // every block, hence every SM, gets the same number of chunks to within one
     const int gstride = gridDim.x * LOOP_GROUPS;
-    const int cbegin = blockIdx.x * LOOP_GROUPS + gi;
+    const int cbegin = blockIdx.x + gridDim.x * gi;
     if (threadIdx.x < A.nsys) sst[threadIdx.x] = *A.sys[threadIdx.x].st;
-    unsigned int gen = 0;
-    if (threadIdx.x == 0) gen = *(volatile unsigned int *)&bar->gen;
-    __syncthreads();
+    unsigned int target = 0;  // the counter is zeroed before every launch
+    __syncthreads();           // the scalar copies in sst are complete
     // phase times of block 0 (thread 0), kept in shared memory
     __shared__ unsigned long long s_tp[6];
     const bool timing = prof != nullptr && blockIdx.x == 0 && threadIdx.x == 0;
@@ -327,7 +337,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
                 S.y[row] = S.invdiag[row] * p;
             }
         }
-        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (!(ok = grid_sync(bar, target, &s_ok))) break;
         mark(0);
         // K2: v = A y, <r0, v>
         for (int c = cbegin; c < A.total_chunks; c += gstride) {
@@ -337,7 +347,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             const int lc = c - S.chunk_begin;
             const int r0 = lc * CH + lane;
             double a = 0.0;
-#pragma unroll 2
+#pragma unroll kSpmvUnroll
             for (int m = 0; m < RPL; ++m) {
                 const int row = r0 + m * LANES;
                 const double v = spmv_row(S, row, S.y);
@@ -347,7 +357,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             const double t = lanes_tree_sum(a, lane, sm[gi], gsync);
             if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
         }
-        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (!(ok = grid_sync(bar, target, &s_ok))) break;
         if (gi < A.nsys && state_active(sst[gi])) {
             const KSys &S = A.sys[gi];
             const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks, S.nchunks, 1, lane, sm[gi], gsync);
@@ -370,7 +380,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
                 S.z[row] = S.invdiag[row] * sv;
             }
         }
-        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (!(ok = grid_sync(bar, target, &s_ok))) break;
         mark(2);
         // K4: t = A z, <t, t>, <t, s>
         for (int c = cbegin; c < A.total_chunks; c += gstride) {
@@ -380,7 +390,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             const int lc = c - S.chunk_begin;
             const int r0 = lc * CH + lane;
             double att = 0.0, ats = 0.0;
-#pragma unroll 2
+#pragma unroll kSpmvUnroll
             for (int m = 0; m < RPL; ++m) {
                 const int row = r0 + m * LANES;
                 const double t = spmv_row(S, row, S.z);
@@ -394,7 +404,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             lanes_tree_sum2(att, ats, lane, sm[gi], tt, ts, gsync);
             if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
         }
-        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (!(ok = grid_sync(bar, target, &s_ok))) break;
         if (gi < A.nsys && state_active(sst[gi])) {
             const KSys &S = A.sys[gi];
             double ftt, fts;
@@ -428,7 +438,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             lanes_tree_sum2(a0r, arr, lane, sm[gi], t0r, trr, gsync);
             if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks)[lc] = make_double2(t0r, trr);
         }
-        if (!(ok = grid_sync(bar, gen, &s_ok))) break;
+        if (!(ok = grid_sync(bar, target, &s_ok))) break;
         if (gi < A.nsys && state_active(sst[gi])) {
             const KSys &S = A.sys[gi];
             double f0r, frr;
@@ -561,10 +571,10 @@ cudaError_t launch_krylov_loop(const KSetArg &A, GridBar *bar, LoopProf *prof, i
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         g_loop_occ = occ;
     }
-    // every block must be resident at once (cooperative launch); small sets
-    // use fewer blocks so that concurrent solves can share the GPU
-    const int need = (A.total_chunks + LOOP_GROUPS - 1) / LOOP_GROUPS;
-    const int grid = std::max(1, std::min(need, device_sm_count() * occ));
+    // every block must be resident at once (cooperative launch): one block
+    // per SM, or one per chunk for small sets (so that concurrent solves can
+    // share the GPU)
+    const int grid = std::max(1, std::min(A.total_chunks, device_sm_count() * occ));
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     KSetArg a = A;
