@@ -30,6 +30,7 @@
 
 #include "device.cuh"
 #include "kernels.h"
+#include "loop.cuh"
 
 namespace ns3d {
 
@@ -236,52 +237,6 @@ __global__ void k_kr_init2(const __grid_constant__ KSetArg A) {
 // The loop ends when every system is done, when a system needs a restart
 // (the host recomputes its residual and launches the loop again), after
 // `max_iters` iterations, or when a grid barrier gives up waiting.
-
-__device__ __forceinline__ unsigned long long global_ns() {
-    unsigned long long t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Grid-wide barrier of a cooperative launch.  The arrival counter only
-// grows: barrier k of a launch ends when it reaches k * gridDim.x, so a
-// waiting block sees the end as soon as the last arrival lands (no reset, no
-// second flag).  The wait gives up after kBarrierLimitNs (or 2^31 polls):
-// the block records the failure in bar->err and returns false, and the
-// kernel stops at once -- so a launch always terminates, and the host
-// reports the error.
-constexpr unsigned long long kBarrierLimitNs = 4000000000ull;
-
-__device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
-    unsigned int v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, int *s_ok) {
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        target += gridDim.x;
-        __threadfence();  // the block's writes (ordered before by the block barrier) become visible
-        atomicAdd(&bar->count, 1u);
-        if ((int)(ld_acquire(&bar->count) - target) < 0) {
-            const unsigned long long t0 = global_ns();
-            unsigned int polls = 0;
-            while ((int)(ld_acquire(&bar->count) - target) < 0) {
-                if ((++polls & 255u) == 0 && (global_ns() - t0 > kBarrierLimitNs || polls > 0x7fffffffu)) {
-                    atomicExch(&bar->err, 1);
-                    ok = 0;
-                    break;
-                }
-            }
-        }
-        __threadfence();
-        *s_ok = ok;
-    }
-    __syncthreads();
-    return *s_ok != 0;
-}
 
 // rows of a chunk in flight per thread in the SpMV phases (register budget)
 #ifndef NS3D_SPMV_UNROLL

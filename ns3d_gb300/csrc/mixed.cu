@@ -9,15 +9,19 @@
 //   k_dc_resid   r64 = b - A64 x (FP64), |r64|^2 (and |b|^2 in round 0);
 //                last block: convergence test, scale = 1/|r64|, inner target
 //   k_m32_init   f = float(r64 * scale); r = r0 = f; d = 0; p = v = 0; |f|^2
-//   k_m32_p/v/s/t/x   the five BiCGSTAB kernels in FP32 on A32 d = f
-//   k_dc_update  x += double(d) / scale
+//   k_m32_loop   the BiCGSTAB iterations in FP32 on A32 d = f (one
+//                persistent cooperative launch per round)
+//   k_dc_step    theta minimizing |r64 - theta A64 delta|, delta = double(d) / scale
+//   k_dc_update  x += theta delta
 // An inner solve stops at its relative target, at the iteration budget, or
 // at a breakdown (|rho| tiny, non-finite scalars); the next round restarts
 // from the new FP64 residual.  iterations() reports the inner iterations.
+#include <atomic>
 #include <cfloat>
 
 #include "device.cuh"
 #include "kernels.h"
+#include "loop.cuh"
 #include "mixed.h"
 
 namespace ns3d {
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(LANES) k_dc_resid(const __grid_constant__ MSet
                     st->done = 0;
                     st->iter = 0;
                     st->info = 0;
-                    st->maxit = dc->maxit - dc->total_iter;
+                    st->maxit = min(dc->inner_cap, dc->maxit - dc->total_iter);
                 }
             }
         }
@@ -228,126 +232,150 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
     }
 }
 
-__global__ void __launch_bounds__(LANES) k_m32_p(const __grid_constant__ MSetArg A) {
-    __shared__ int sh[4];
-    NS3D_MCHUNK_LOOP(true)
-        const float beta = (float)__ldcg(&S.st->beta), w = (float)__ldcg(&S.st->w);
-        const RowF4 r = ldf4(S.r + r0), v = ldf4(S.v + r0), iv = ldf4(S.invdiag32 + r0);
-        RowF4 p = ldf4(S.p + r0), y;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            p.v[m] = __fmaf_rn(beta, __fmaf_rn(-w, v.v[m], p.v[m]), r.v[m]);
-            y.v[m] = iv.v[m] * p.v[m];
-        }
-        stf4(S.p + r0, p);
-        stf4(S.y + r0, y);
-    }
-}
+// ---- the FP32 inner iterations as one persistent cooperative kernel ----------
+// Same block shape, chunk interleaving, partial regions and grid barrier as
+// the FP64 loop kernel (krylov.cu); its phases are those of the FP64 loop
+// with FP32 vectors, FP32 lane accumulation and FP64 trees and scalars.  Every
+// block keeps a copy of the inner state; the kernel ends when every inner
+// solve of the round is done or after `max_iters` iterations.
+__device__ __forceinline__ bool inner_active(const KState &k, int dc_done) { return !dc_done && !k.done; }
 
-__global__ void __launch_bounds__(LANES) k_m32_v(const __grid_constant__ MSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    NS3D_MCHUNK_LOOP(true)
-        float a = 0.0f;
+__global__ void __launch_bounds__(LOOP_THREADS, 1)
+    k_m32_loop(const __grid_constant__ MSetArg A, GridBar *bar, int max_iters) {
+    __shared__ KState sst[KMAX];
+    __shared__ int sdc[KMAX];
+    __shared__ double sm[LOOP_GROUPS][LANES];
+    __shared__ int s_ok;
+    const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
+    const GroupSync gsync{gi + 1};
+    const int gstride = gridDim.x * LOOP_GROUPS;
+    const int cbegin = blockIdx.x + gridDim.x * gi;
+    if (threadIdx.x < A.nsys) {
+        sst[threadIdx.x] = *A.sys[threadIdx.x].st;
+        sdc[threadIdx.x] = A.sys[threadIdx.x].dc->done;
+    }
+    unsigned int target = 0;
+    __syncthreads();
+    int it = 0;
+    for (; it < max_iters; ++it) {
+        // p = r + beta (p - w v); y = D^-1 p
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = msys_of_chunk(A, c);
+            if (!inner_active(sst[si], sdc[si])) continue;
+            const MSys &S = A.sys[si];
+            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const float beta = (float)sst[si].beta, w = (float)sst[si].w;
 #pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            const int row = r0 + m * LANES;
-            const float v = spmv_f32_row(S, row, S.y);
-            S.v[row] = v;
-            if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
-        }
-        const double t = block_tree_sum((double)a, sm);
-        if (threadIdx.x == 0) S.part[2 * (size_t)lc] = t;
-        if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
-            const double d = final_partials_sum(S.part, S.nchunks, 2, sm);
-            if (threadIdx.x == 0) {
-                S.st->counter = 0;
-                S.st->alpha = S.st->rho / d;
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const float p = __fmaf_rn(beta, __fmaf_rn(-w, S.v[row], S.p[row]), S.r[row]);
+                S.p[row] = p;
+                S.y[row] = S.invdiag32[row] * p;
             }
         }
-    }
-}
-
-__global__ void __launch_bounds__(LANES) k_m32_s(const __grid_constant__ MSetArg A) {
-    __shared__ int sh[4];
-    NS3D_MCHUNK_LOOP(true)
-        const float alpha = (float)__ldcg(&S.st->alpha);
-        const RowF4 r = ldf4(S.r + r0), v = ldf4(S.v + r0), iv = ldf4(S.invdiag32 + r0);
-        RowF4 s, z;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            s.v[m] = __fmaf_rn(-alpha, v.v[m], r.v[m]);
-            z.v[m] = iv.v[m] * s.v[m];
+        if (!grid_sync(bar, target, &s_ok)) break;
+        // v = A y, <r0, v>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = msys_of_chunk(A, c);
+            if (!inner_active(sst[si], sdc[si])) continue;
+            const MSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            float a = 0.0f;
+#pragma unroll 2
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const float v = spmv_f32_row(S, row, S.y);
+                S.v[row] = v;
+                if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
+            }
+            const double t = lanes_tree_sum((double)a, lane, sm[gi], gsync);
+            if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
         }
-        stf4(S.s + r0, s);
-        stf4(S.z + r0, z);
-    }
-}
-
-__global__ void __launch_bounds__(LANES) k_m32_t(const __grid_constant__ MSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    NS3D_MCHUNK_LOOP(true)
-        float att = 0.0f, ats = 0.0f;
+        if (!grid_sync(bar, target, &s_ok)) break;
+        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+            const MSys &S = A.sys[gi];
+            const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks, S.nchunks, 1, lane, sm[gi], gsync);
+            if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+        }
+        __syncthreads();
+        // s = r - alpha v; z = D^-1 s
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = msys_of_chunk(A, c);
+            if (!inner_active(sst[si], sdc[si])) continue;
+            const MSys &S = A.sys[si];
+            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const float alpha = (float)sst[si].alpha;
 #pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            const int row = r0 + m * LANES;
-            const float t = spmv_f32_row(S, row, S.z);
-            S.t[row] = t;
-            if (row < S.n) {
-                att = __fmaf_rn(t, t, att);
-                ats = __fmaf_rn(t, S.s[row], ats);
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const float sv = __fmaf_rn(-alpha, S.v[row], S.r[row]);
+                S.s[row] = sv;
+                S.z[row] = S.invdiag32[row] * sv;
             }
         }
-        double tt, ts;
-        block_tree_sum2((double)att, (double)ats, sm, tt, ts);
-        if (threadIdx.x == 0) {
-            S.part[2 * (size_t)lc + 0] = tt;
-            S.part[2 * (size_t)lc + 1] = ts;
+        if (!grid_sync(bar, target, &s_ok)) break;
+        // t = A z, <t, t>, <t, s>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = msys_of_chunk(A, c);
+            if (!inner_active(sst[si], sdc[si])) continue;
+            const MSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            float att = 0.0f, ats = 0.0f;
+#pragma unroll 2
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                const float t = spmv_f32_row(S, row, S.z);
+                S.t[row] = t;
+                if (row < S.n) {
+                    att = __fmaf_rn(t, t, att);
+                    ats = __fmaf_rn(t, S.s[row], ats);
+                }
+            }
+            double tt, ts;
+            lanes_tree_sum2((double)att, (double)ats, lane, sm[gi], tt, ts, gsync);
+            if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
         }
-        if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
+        if (!grid_sync(bar, target, &s_ok)) break;
+        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+            const MSys &S = A.sys[gi];
             double ftt, fts;
-            final_partials_sum2(S.part, S.nchunks, sm, ftt, fts);
-            if (threadIdx.x == 0) {
-                S.st->counter = 0;
-                S.st->w = (ftt > 0.0) ? fts / ftt : 0.0;
+            lanes_final_sum2(S.part, S.nchunks, lane, sm[gi], ftt, fts, gsync);
+            if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+        }
+        __syncthreads();
+        // x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
+        for (int c = cbegin; c < A.total_chunks; c += gstride) {
+            const int si = msys_of_chunk(A, c);
+            if (!inner_active(sst[si], sdc[si])) continue;
+            const MSys &S = A.sys[si];
+            const int lc = c - S.chunk_begin;
+            const int r0 = lc * CH + lane;
+            const float alpha = (float)sst[si].alpha, w = (float)sst[si].w;
+            float a0r = 0.0f, arr = 0.0f;
+#pragma unroll 2
+            for (int m = 0; m < RPL; ++m) {
+                const int row = r0 + m * LANES;
+                S.x[row] = __fmaf_rn(w, S.z[row], __fmaf_rn(alpha, S.y[row], S.x[row]));
+                const float r = __fmaf_rn(-w, S.t[row], S.s[row]);
+                S.r[row] = r;
+                if (row < S.n) {
+                    a0r = __fmaf_rn(S.r0[row], r, a0r);
+                    arr = __fmaf_rn(r, r, arr);
+                }
             }
+            double t0r, trr;
+            lanes_tree_sum2((double)a0r, (double)arr, lane, sm[gi], t0r, trr, gsync);
+            if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks)[lc] = make_double2(t0r, trr);
         }
-    }
-}
-
-__global__ void __launch_bounds__(LANES) k_m32_x(const __grid_constant__ MSetArg A) {
-    __shared__ double sm[LANES];
-    __shared__ int sh[4];
-    NS3D_MCHUNK_LOOP(true)
-        const float alpha = (float)__ldcg(&S.st->alpha), w = (float)__ldcg(&S.st->w);
-        const RowF4 y = ldf4(S.y + r0), z = ldf4(S.z + r0), t = ldf4(S.t + r0), s = ldf4(S.s + r0);
-        const RowF4 rr0 = ldf4(S.r0 + r0);
-        RowF4 x = ldf4(S.x + r0), r;
-        float a0r = 0.0f, arr = 0.0f;
-#pragma unroll
-        for (int m = 0; m < RPL; ++m) {
-            x.v[m] = __fmaf_rn(w, z.v[m], __fmaf_rn(alpha, y.v[m], x.v[m]));
-            r.v[m] = __fmaf_rn(-w, t.v[m], s.v[m]);
-            if (r0 + m * LANES < S.n) {
-                a0r = __fmaf_rn(rr0.v[m], r.v[m], a0r);
-                arr = __fmaf_rn(r.v[m], r.v[m], arr);
-            }
-        }
-        stf4(S.x + r0, x);
-        stf4(S.r + r0, r);
-        double t0r, trr;
-        block_tree_sum2((double)a0r, (double)arr, sm, t0r, trr);
-        if (threadIdx.x == 0) {
-            S.part[2 * (size_t)lc + 0] = t0r;
-            S.part[2 * (size_t)lc + 1] = trr;
-        }
-        if (m_arrive_last(&S.st->counter, (unsigned)S.nchunks, sh)) {
+        if (!grid_sync(bar, target, &s_ok)) break;
+        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+            const MSys &S = A.sys[gi];
             double f0r, frr;
-            final_partials_sum2(S.part, S.nchunks, sm, f0r, frr);
-            if (threadIdx.x == 0) {
-                KState *st = S.st;
-                st->counter = 0;
+            lanes_final_sum2(S.part + 2 * (size_t)S.nchunks, S.nchunks, lane, sm[gi], f0r, frr, gsync);
+            if (lane == 0) {
+                KState *st = &sst[gi];
                 st->rr = frr;
                 st->iter += 1;
                 st->work += 1;
@@ -365,6 +393,62 @@ __global__ void __launch_bounds__(LANES) k_m32_x(const __grid_constant__ MSetArg
                 }
             }
         }
+        __syncthreads();
+        bool any = false;
+        for (int q = 0; q < A.nsys; ++q) any = any || inner_active(sst[q], sdc[q]);
+        if (!any) {
+            ++it;
+            break;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x < A.nsys) {
+        KState k = sst[threadIdx.x];
+        k.counter = 0;
+        *A.sys[threadIdx.x].st = k;
+    }
+}
+
+// Step length of the round's correction delta = double(d) / scale:
+// theta = <r64, A64 delta> / <A64 delta, A64 delta> minimizes the FP64
+// residual along delta, so a correction from an inaccurate FP32 solve can
+// shrink the residual less but never grow it.  The last block to finish
+// sets dc->theta.
+__global__ void __launch_bounds__(LANES) k_dc_step(const __grid_constant__ MSetArg A) {
+    __shared__ double sm[LANES];
+    __shared__ int sh[4];
+    for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
+        const MSys &S = A.sys[msys_of_chunk(A, c)];
+        if (!(__ldcg(&S.dc->done) == 0 && __ldcg(&S.st->info) == 0)) continue;
+        const double inv = 1.0 / __ldcg(&S.dc->scale);
+        const int lc = c - S.chunk_begin;
+        const int r0 = lc * CH + threadIdx.x;
+        const size_t np = (size_t)S.npad;
+        double arq = 0.0, aqq = 0.0;
+        for (int m = 0; m < RPL; ++m) {
+            const int row = r0 + m * LANES;
+            const int *nb = S.nbr + row;
+            const double *cf = S.coef64 + row;
+            const double q = row_ordered(row, nb[0 * np], nb[1 * np], nb[2 * np], nb[3 * np], nb[4 * np], nb[5 * np],
+                                         [&](double acc, int sl, int col) {
+                                             return __fma_rn(cf[(size_t)sl * np], (double)S.x[col] * inv, acc);
+                                         });
+            if (row < S.n) {
+                arq = __fma_rn(S.r64[row], q, arq);
+                aqq = __fma_rn(q, q, aqq);
+            }
+        }
+        double trq, tqq;
+        block_tree_sum2(arq, aqq, sm, trq, tqq);
+        if (threadIdx.x == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(trq, tqq);
+        if (m_arrive_last(&S.dc->counter, (unsigned)S.nchunks, sh)) {
+            double frq, fqq;
+            final_partials_sum2(S.part, S.nchunks, sm, frq, fqq);
+            if (threadIdx.x == 0) {
+                S.dc->counter = 0;
+                const double th = (fqq > 0.0) ? frq / fqq : 0.0;
+                S.dc->theta = finite(th) ? th : 0.0;
+            }
+        }
     }
 }
 
@@ -373,11 +457,12 @@ __global__ void k_dc_update(const __grid_constant__ MSetArg A) {
         const MSys &S = A.sys[msys_of_chunk(A, c)];
         if (!(__ldcg(&S.dc->done) == 0 && __ldcg(&S.st->info) == 0)) continue;
         const double inv = 1.0 / __ldcg(&S.dc->scale);
+        const double theta = __ldcg(&S.dc->theta);
         const int r0 = (c - S.chunk_begin) * CH + threadIdx.x;
 #pragma unroll
         for (int m = 0; m < RPL; ++m) {
             const int row = r0 + m * LANES;
-            S.x64[row] = __fma_rn((double)S.x[row], inv, S.x64[row]);
+            S.x64[row] = __fma_rn(theta, (double)S.x[row] * inv, S.x64[row]);
         }
     }
 }
@@ -421,20 +506,31 @@ void launch_m32_init(const MSetArg &A, cudaStream_t st) {
     k_m32_init<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
-void launch_m32_iteration(const MSetArg &A, cudaStream_t st) {
-    if (A.total_chunks <= 0) return;
-    const int g = m_grid(A.total_chunks);
-    count_launches(5);
-    k_m32_p<<<g, LANES, 0, st>>>(A);
-    k_m32_v<<<g, LANES, 0, st>>>(A);
-    k_m32_s<<<g, LANES, 0, st>>>(A);
-    k_m32_t<<<g, LANES, 0, st>>>(A);
-    k_m32_x<<<g, LANES, 0, st>>>(A);
+
+static std::atomic<int> g_m32_occ{0};
+
+cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaStream_t st) {
+    if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
+    int occ = g_m32_occ.load();
+    if (occ == 0) {
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_m32_loop, LOOP_THREADS, 0);
+        if (e != cudaSuccess) return e;
+        if (occ <= 0) return cudaErrorLaunchOutOfResources;
+        g_m32_occ = occ;
+    }
+    const int grid = std::max(1, std::min(A.total_chunks, device_sm_count() * occ));
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
+    if (e != cudaSuccess) return e;
+    MSetArg a = A;
+    void *args[] = {&a, &bar, &max_iters};
+    count_launches(1);
+    return cudaLaunchCooperativeKernel((const void *)k_m32_loop, grid, LOOP_THREADS, args, 0, st);
 }
 
 void launch_dc_update(const MSetArg &A, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
-    count_launches(1);
+    count_launches(2);
+    k_dc_step<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
     k_dc_update<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 

@@ -8,7 +8,9 @@ namespace ns3d {
 // FP64 defect-correction state of one system
 struct DCState {
     double rr, bb, tol, tol2, scale, error, tin, tin_min;
-    int total_iter, maxit, done, info, zero_rhs, pad_;
+    double theta;    // step length of the current correction (minimal FP64 residual)
+    int total_iter, maxit, done, info, zero_rhs;
+    int inner_cap;   // FP32 iterations allowed per round
     unsigned int counter, pad2_;
 };
 
@@ -36,7 +38,10 @@ void launch_to_f32(const double *coef, const double *invdiag, int npad, float *c
                    cudaStream_t st);
 void launch_dc_resid(const MSetArg &set, int first, cudaStream_t st);
 void launch_m32_init(const MSetArg &set, cudaStream_t st);
-void launch_m32_iteration(const MSetArg &set, cudaStream_t st);
+// FP32 inner iterations until every inner solve of the round is done
+cudaError_t launch_m32_loop(const MSetArg &set, GridBar *bar, int max_iters, cudaStream_t st);
+// theta = <r, A d> / <A d, A d> for the FP32 correction d (FP64 SpMV), then
+// x += theta d
 void launch_dc_update(const MSetArg &set, cudaStream_t st);
 
 }  // namespace ns3d

@@ -25,6 +25,10 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     if (ns > KMAX) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     std::vector<MSys> ms(ns);
     int chunk = 0;
+    if (!bar_.n) {
+        bar_.alloc_zero(1, st);
+        h_err_.alloc(1);
+    }
     if ((int)st_.n < ns) {
         st_.alloc_zero(ns, st);
         out_st_.alloc_zero(ns, st);
@@ -78,6 +82,7 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
         d.tol = items[i].tol;
         d.maxit = items[i].maxit;
         d.tin_min = inner_rel_tol;
+        d.inner_cap = inner_cap;
         if (S.n == 0) {
             d.done = 1;
             d.zero_rhs = 1;
@@ -97,34 +102,22 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
     // maxit + 2 rounds bound the loop; each round's inner loop is bounded by
     // the remaining iteration budget.
     long rounds = 0;
-    int work_total = 0;
-    std::vector<int> work(ns, 0);
+    // One round = FP32 init, the FP32 loop kernel (it ends when every inner
+    // solve of the round is done: each is capped by the remaining iteration
+    // budget), the FP64 update and residual; the host reads the outer state
+    // once per round.
     while (true) {
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_dc_.p, dc_.p, ns * sizeof(DCState), cudaMemcpyDeviceToHost, st));
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(h_err_.p, &bar_.p->err, sizeof(int), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+        if (rounds > 0 && h_err_.p[0])
+            throw ApiError(NS3D_ERR_TIMEOUT, "FP32 BiCGSTAB loop kernel: a grid barrier timed out");
         bool all_done = true;
         for (int i = 0; i < ns; ++i) all_done = all_done && h_dc_.p[i].done;
         if (all_done) break;
         if (++rounds > maxit + 2L) throw ApiError(NS3D_ERR_TIMEOUT, "defect correction exceeded its round bound");
         launch_m32_init(set_, st);
-        long issued = 0;
-        int batch = std::max(1, std::min(32, prev_iters_ / 2));
-        while (true) {
-            for (int b = 0; b < batch; ++b) launch_m32_iteration(set_, st);
-            issued += batch;
-            batch = std::min(64, batch * 2);
-            NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
-            NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
-            bool inner_done = true;
-            for (int i = 0; i < ns; ++i)
-                if (!h_dc_.p[i].done && !h_st_.p[i].done) inner_done = false;
-            if (inner_done) break;
-            if (issued > maxit + 64L) throw ApiError(NS3D_ERR_TIMEOUT, "FP32 BiCGSTAB exceeded its iteration bound");
-        }
-        int round_max = 0;
-        for (int i = 0; i < ns; ++i)
-            if (!h_dc_.p[i].done) round_max = std::max(round_max, h_st_.p[i].iter);
-        prev_iters_ = std::max(2, round_max);
+        NS3D_CUDA_CHECK(launch_m32_loop(set_, bar_.p, maxit + 64, st));
         launch_dc_update(set_, st);
         launch_dc_resid(set_, 0, st);
     }
@@ -144,9 +137,7 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
         k.info = d.info;
         k.done = 1;
         h_out_.p[i] = k;
-        work_total += out[i].work;
     }
-    (void)work_total;
     NS3D_CUDA_CHECK(cudaMemcpyAsync(out_st_.p, h_out_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
 }
 

@@ -169,6 +169,7 @@ class MixedSet {
     // velocity post-processing kernel
     const KState *device_state(int i) const { return out_st_.p + i; }
     double inner_rel_tol = 1e-4;  // floor of the per-round FP32 reduction target
+    int inner_cap = 400;          // FP32 iterations per round at most
     ~MixedSet() = default;
 
   private:
@@ -179,6 +180,8 @@ class MixedSet {
     HBuf<DCState> h_dc_;
     std::vector<const double *> key_;
     MSetArg set_;  // passed to every kernel by value
+    DBuf<GridBar> bar_;
+    HBuf<int> h_err_;
     int nsys_ = 0, total_chunks_ = 0;
     int prev_iters_ = 8;
 };
