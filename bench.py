@@ -190,6 +190,105 @@ def cpu_sample(capi, img, method, outer):
     return dt, r.krylov_rows, r
 
 
+# Serving sample: a seeded stream of permeability requests (the serving
+# workload's mix, with edges bounded so the sample ends within about a
+# minute; --serving-requests and --serving-edge widen it):
+# image edges log-uniform in SERVE_EDGE, sphere packs (radius 3-8, porosity
+# 0.35-0.9) or fibre packs (radius 2-4, porosity 0.7-0.95), flow along x, y
+# or z, SIMPLEC or IDEAL, Poisson arrivals at SERVE_RATE requests/s.
+SERVE_REQUESTS = 12
+SERVE_EDGE = (32, 56)
+SERVE_RATE = 8.0
+SERVE_ACTIVE = 4
+
+
+def serving_requests(capi, lib, n, seed=7):
+    from ns3d_gb300 import synth
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(n):
+        shape = tuple(int(round(np.exp(rng.uniform(np.log(SERVE_EDGE[0]), np.log(SERVE_EDGE[1]))))) for _ in range(3))
+        if rng.integers(2) == 0:
+            img, info = synth.rsa_spheres(shape, int(rng.integers(3, 9)), float(rng.uniform(0.35, 0.9)), seed + 100 + i)
+            kind = "spheres"
+        else:
+            img, info = synth.random_fibres(shape, int(rng.integers(2, 5)), float(rng.uniform(0.7, 0.95)),
+                                            seed + 100 + i)
+            kind = "fibres"
+        direction = int(rng.integers(1, 4))
+        method = [0, 3][int(rng.integers(2))]  # SIMPLEC or IDEAL
+        reqs.append({"img": img, "raw": synth.to_raw(img), "shape": shape, "kind": kind, "phi": info["porosity"],
+                     "direction": direction, "method": method})
+    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, size=n))
+    return reqs, arrivals - arrivals[0]
+
+
+def request_params(capi, lib, r, precision):
+    dx = 1e-6
+    ext = r["shape"][r["direction"] - 1]
+    return capi.default_params(lib, dx=dx, dy=-1.0, dz=-1.0, mu=1e-3, rho=1.0, p0=1.0, gradp=1.0 / (ext * dx),
+                               alpha=0.5, beta=1.0, vsolvertol=1e-8, psolvertol=1e-8, pcsolvertol=1e-8,
+                               simpletol=1e-6, maxitsolver=2000, maxitSIMPLE=MAX_OUTER, N1=2, N2=2, porevalue=0,
+                               direction=r["direction"], border=0, method=r["method"], precision=precision)
+
+
+def run_serving(capi, lib):
+    """Plain FP64 one request at a time vs the continuous-batching server in
+    mixed precision (and in FP64) on the same request stream."""
+    reqs, arrivals = serving_requests(capi, lib, SERVE_REQUESTS)
+    # plain FP64, one at a time
+    k64, t64 = [], 0.0
+    for r in reqs:
+        s = capi.Solver(lib, request_params(capi, lib, r, 0), r["raw"], r["shape"])
+        t = time.perf_counter()
+        res = s.solve()
+        t64 += time.perf_counter() - t
+        k64.append(res.K)
+        s.close()
+
+    def serve(precision):
+        srv = capi.Server(lib, SERVE_ACTIVE)
+        t0 = time.perf_counter()
+        tickets = []
+        for r, a in zip(reqs, arrivals):
+            now = time.perf_counter() - t0
+            if a > now:
+                time.sleep(a - now)
+            tickets.append(srv.submit(request_params(capi, lib, r, precision), r["raw"], r["shape"]))
+        ks, lats = [], []
+        for t in tickets:
+            res, lat = srv.wait(t)
+            ks.append(res.K)
+            lats.append(lat)
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        srv.stop()
+        return ks, lats, wall, st
+
+    kmx, lmx, wmx, smx = serve(1)
+    kfp, lfp, wfp, sfp = serve(0)
+    rel = [abs(a - b) / abs(b) for a, b in zip(kmx, k64)]
+    rel_fp = [abs(a - b) / abs(b) for a, b in zip(kfp, k64)]
+    n = len(reqs)
+    cells = sum(int(np.prod(r["shape"])) for r in reqs)
+    return {
+        "workload": "%d seeded requests, edges log-uniform %d-%d, spheres (r 3-8, phi 0.35-0.9) or fibres "
+                    "(r 2-4, phi 0.7-0.95), flow x/y/z, SIMPLEC or IDEAL, Poisson arrivals %.1f/s, "
+                    "up to %d solves in flight" % (n, SERVE_EDGE[0], SERVE_EDGE[1], SERVE_RATE, SERVE_ACTIVE),
+        "voxels": cells,
+        "plain_fp64_one_at_a_time": {"solves_per_s": n / t64, "seconds": t64},
+        "served_mixed": {"solves_per_s": n / wmx, "seconds": wmx, "p50_latency_s": float(np.percentile(lmx, 50)),
+                         "p99_latency_s": float(np.percentile(lmx, 99)), "peak_active": smx.peak_active,
+                         "max_K_rel_err_vs_fp64": max(rel), "K_rel_err_vs_fp64": rel,
+                         "speedup_vs_plain_fp64": (n / wmx) / (n / t64)},
+        "served_fp64": {"solves_per_s": n / wfp, "seconds": wfp, "p50_latency_s": float(np.percentile(lfp, 50)),
+                        "p99_latency_s": float(np.percentile(lfp, 99)), "peak_active": sfp.peak_active,
+                        "max_K_rel_err_vs_fp64": max(rel_fp),
+                        "speedup_vs_plain_fp64": (n / wfp) / (n / t64)},
+        "note": "wall time of the served runs includes the Poisson arrival gaps (%.2f s spread)" % arrivals[-1],
+    }
+
+
 def run_reference(args):
     from ns3d_gb300 import capi
     world, rank, _, dist = dist_setup()
@@ -275,7 +374,7 @@ def run_gpu(args):
     ks = {METHODS[i % len(METHODS)]: float(results[i].K) for i in range(len(results))}
     cell_updates = sum(sizes.np * (r.iterations + 1) for r in results)
     # end to end through the C-ABI with host buffers
-    e2e_steps = 0 if args.no_e2e else min(args.steps, len(METHODS))
+    e2e_steps = 0 if args.no_e2e else min(args.steps, 2)
     h2d = raw.nbytes
     d2h = 8 * (sizes.np + sizes.nu + sizes.nv + sizes.nw)
     barrier(dist)
@@ -289,6 +388,9 @@ def run_gpu(args):
         assert f[0].size == sizes.np
     e2e_elapsed = reduce_max(dist, time.perf_counter() - t1)
     e2e_value = world * e2e_steps / e2e_elapsed if e2e_steps else None
+    serving = None
+    if args.serving and world == 1:
+        serving = run_serving(capi, lib)
     line = None
     if rank == 0:
         cpu = None
@@ -330,6 +432,7 @@ def run_gpu(args):
                 "gpu_launches": gpu_launches,
                 "krylov_rows": kr_rows,
                 "cpu_baseline": cpu,
+                "serving": serving,
                 "clocks": clk}
         print(json.dumps(line))
     for s in solvers.values():
@@ -340,7 +443,7 @@ def run_gpu(args):
 
 
 def main():
-    global METHODS, MAX_OUTER, PRECISION
+    global METHODS, MAX_OUTER, PRECISION, SERVE_REQUESTS, SERVE_EDGE, SERVE_ACTIVE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -348,11 +451,19 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
+    ap.add_argument("--no-serving", dest="serving", action="store_false",
+                    help="skip the serving sample (plain FP64 one at a time vs the mixed-precision server)")
+    ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--serving-edge", default="%d,%d" % SERVE_EDGE, help="min,max image edge of the requests")
+    ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
+    SERVE_REQUESTS = args.serving_requests
+    SERVE_EDGE = tuple(int(x) for x in args.serving_edge.split(","))
+    SERVE_ACTIVE = args.serving_active
     METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]
     MAX_OUTER = args.max_outer
     PRECISION = 1 if args.precision == "mixed" else 0

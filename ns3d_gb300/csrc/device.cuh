@@ -113,9 +113,13 @@ struct KSys {  // one system of a solve set (device array)
     const double *invdiag;
     const double *b;
     double *x, *r, *r0, *p, *v, *y, *s, *z, *t;
-    double *part;  // [5 * nchunks]: reduction partials (layout in krylov.cu)
+    double *part;  // [PART_PER_CHUNK * nchunks]: reduction partials (layout in krylov.cu)
     KState *st;
 };
+
+// chunk partials held per system (the FP64 loop uses 5 per chunk, the FP32
+// loop 5 per quarter chunk)
+constexpr int PART_PER_CHUNK = 20;
 
 // A solve set as a kernel argument (passed by value, read from constant
 // memory): the systems in chunk order, sys[0].chunk_begin == 0.
@@ -131,6 +135,9 @@ struct KSetArg {
 #endif
 constexpr int LOOP_THREADS = NS3D_LOOP_THREADS;
 constexpr int LOOP_GROUPS = LOOP_THREADS / LANES;
+// blocks per SM the loop kernels are compiled for (64 registers a thread)
+constexpr int LOOP_MIN_BLOCKS = LOOP_THREADS >= 1024 ? 1 : 1024 / LOOP_THREADS;
+static_assert(LOOP_GROUPS >= KMAX, "group s combines the partials of system s");
 struct GridBar {  // arrival counter and error flag on separate 128-byte lines
     unsigned int count, pad0_[31];
     int err, pad1_[31];

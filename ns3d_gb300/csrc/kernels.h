@@ -78,6 +78,15 @@ void launch_krylov_init(const KSetArg &set, cudaStream_t st);
 // iterations until every system is done, one needs a restart, or max_iters
 cudaError_t launch_krylov_loop(const KSetArg &set, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st);
 void launch_krylov_restart(const KSetArg &set, cudaStream_t st);
+// blocks of a loop-kernel launch over `units` work units, units_per_chunk
+// of them per 1024-row chunk (occ blocks per SM)
+int loop_grid(int units, int units_per_chunk, int occ);
+// solves running in this process (ns3d_solve calls in flight)
+struct ActiveSolve {
+    ActiveSolve();
+    ~ActiveSolve();
+};
+int active_solves();
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st);
 int device_sm_count();
 // kernels launched by this library since it was loaded

@@ -246,7 +246,7 @@ constexpr int kSpmvUnroll = NS3D_SPMV_UNROLL;
 
 __device__ __forceinline__ bool state_active(const KState &k) { return (k.done | k.paused) == 0; }
 
-__global__ void __launch_bounds__(LOOP_THREADS, 1)
+__global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     k_kr_loop(const __grid_constant__ KSetArg A, GridBar *bar, LoopProf *prof, int max_iters) {
     __shared__ KState sst[KMAX];
     __shared__ double sm[LOOP_GROUPS][LANES];
@@ -515,6 +515,29 @@ void launch_krylov_init(const KSetArg &A, cudaStream_t st) {
     k_kr_init2<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
+// Blocks of a loop-kernel launch.  Every block must be resident at once
+// (cooperative launch).  A solve that runs alone spreads its work units over
+// every SM (one block per SM).  While k solves run in the process, a solve
+// takes about 1/k of the SMs -- but at least one block per LOOP_GROUPS
+// chunks of rows, so that no group holds more than one chunk per phase --
+// and the loop kernels of concurrent solves, on their own streams, run side
+// by side.
+static std::atomic<int> g_active_solves{0};
+ActiveSolve::ActiveSolve() { g_active_solves++; }
+ActiveSolve::~ActiveSolve() { g_active_solves--; }
+int active_solves() { return g_active_solves.load(); }
+
+int loop_grid(int units, int units_per_chunk, int occ) {
+    const int slots = device_sm_count() * std::max(occ, 1);
+    const int active = std::max(1, g_active_solves.load());
+    if (active == 1) return std::max(1, std::min(units, slots));
+    // a fair share of the SMs, but never more than one chunk of rows per group
+    const int per_block = LOOP_GROUPS * std::max(units_per_chunk, 1);
+    const int dense = (units + per_block - 1) / per_block;
+    const int fair = std::max(1, slots / active);
+    return std::max(1, std::min(std::max(dense, std::min(fair, units)), slots));
+}
+
 static std::atomic<int> g_loop_occ{0};
 
 cudaError_t launch_krylov_loop(const KSetArg &A, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st) {
@@ -526,10 +549,7 @@ cudaError_t launch_krylov_loop(const KSetArg &A, GridBar *bar, LoopProf *prof, i
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         g_loop_occ = occ;
     }
-    // every block must be resident at once (cooperative launch): one block
-    // per SM, or one per chunk for small sets (so that concurrent solves can
-    // share the GPU)
-    const int grid = std::max(1, std::min(A.total_chunks, device_sm_count() * occ));
+    const int grid = loop_grid(A.total_chunks, 1, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     KSetArg a = A;

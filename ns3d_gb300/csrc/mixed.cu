@@ -233,14 +233,17 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
 }
 
 // ---- the FP32 inner iterations as one persistent cooperative kernel ----------
-// Same block shape, chunk interleaving, partial regions and grid barrier as
-// the FP64 loop kernel (krylov.cu); its phases are those of the FP64 loop
-// with FP32 vectors, FP32 lane accumulation and FP64 trees and scalars.  Every
+// Same block shape, interleaving, partial regions and grid barrier as the
+// FP64 loop kernel (krylov.cu); its phases are those of the FP64 loop with
+// FP32 vectors, FP32 lane accumulation and FP64 trees and scalars.  The FP32
+// results follow no fixed-order contract, so the work unit is a quarter
+// chunk (MUNIT = 256 rows, MRPL = 2 per lane): a group finishes a unit in one
+// round of loads, and a small system spreads over 4x more groups.  Every
 // block keeps a copy of the inner state; the kernel ends when every inner
 // solve of the round is done or after `max_iters` iterations.
 __device__ __forceinline__ bool inner_active(const KState &k, int dc_done) { return !dc_done && !k.done; }
 
-__global__ void __launch_bounds__(LOOP_THREADS, 1)
+__global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     k_m32_loop(const __grid_constant__ MSetArg A, GridBar *bar, int max_iters) {
     __shared__ KState sst[KMAX];
     __shared__ int sdc[KMAX];
@@ -250,6 +253,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
     const GroupSync gsync{gi + 1};
     const int gstride = gridDim.x * LOOP_GROUPS;
     const int cbegin = blockIdx.x + gridDim.x * gi;
+    const int total_units = A.total_chunks * MSUB;
     if (threadIdx.x < A.nsys) {
         sst[threadIdx.x] = *A.sys[threadIdx.x].st;
         sdc[threadIdx.x] = A.sys[threadIdx.x].dc->done;
@@ -259,14 +263,14 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
     int it = 0;
     for (; it < max_iters; ++it) {
         // p = r + beta (p - w v); y = D^-1 p
-        for (int c = cbegin; c < A.total_chunks; c += gstride) {
-            const int si = msys_of_chunk(A, c);
+        for (int u = cbegin; u < total_units; u += gstride) {
+            const int si = msys_of_chunk(A, u / MSUB);
             if (!inner_active(sst[si], sdc[si])) continue;
             const MSys &S = A.sys[si];
-            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
             const float beta = (float)sst[si].beta, w = (float)sst[si].w;
 #pragma unroll
-            for (int m = 0; m < RPL; ++m) {
+            for (int m = 0; m < MRPL; ++m) {
                 const int row = r0 + m * LANES;
                 const float p = __fmaf_rn(beta, __fmaf_rn(-w, S.v[row], S.p[row]), S.r[row]);
                 S.p[row] = p;
@@ -275,39 +279,39 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         // v = A y, <r0, v>
-        for (int c = cbegin; c < A.total_chunks; c += gstride) {
-            const int si = msys_of_chunk(A, c);
+        for (int u = cbegin; u < total_units; u += gstride) {
+            const int si = msys_of_chunk(A, u / MSUB);
             if (!inner_active(sst[si], sdc[si])) continue;
             const MSys &S = A.sys[si];
-            const int lc = c - S.chunk_begin;
-            const int r0 = lc * CH + lane;
+            const int lc = u - S.chunk_begin * MSUB;
+            const int r0 = lc * MUNIT + lane;
             float a = 0.0f;
-#pragma unroll 2
-            for (int m = 0; m < RPL; ++m) {
+#pragma unroll
+            for (int m = 0; m < MRPL; ++m) {
                 const int row = r0 + m * LANES;
                 const float v = spmv_f32_row(S, row, S.y);
                 S.v[row] = v;
                 if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
             }
             const double t = lanes_tree_sum((double)a, lane, sm[gi], gsync);
-            if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
+            if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = t;
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
             const MSys &S = A.sys[gi];
-            const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks, S.nchunks, 1, lane, sm[gi], gsync);
+            const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
             if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
         }
         __syncthreads();
         // s = r - alpha v; z = D^-1 s
-        for (int c = cbegin; c < A.total_chunks; c += gstride) {
-            const int si = msys_of_chunk(A, c);
+        for (int u = cbegin; u < total_units; u += gstride) {
+            const int si = msys_of_chunk(A, u / MSUB);
             if (!inner_active(sst[si], sdc[si])) continue;
             const MSys &S = A.sys[si];
-            const int r0 = (c - S.chunk_begin) * CH + lane;
+            const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
             const float alpha = (float)sst[si].alpha;
 #pragma unroll
-            for (int m = 0; m < RPL; ++m) {
+            for (int m = 0; m < MRPL; ++m) {
                 const int row = r0 + m * LANES;
                 const float sv = __fmaf_rn(-alpha, S.v[row], S.r[row]);
                 S.s[row] = sv;
@@ -316,15 +320,15 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         // t = A z, <t, t>, <t, s>
-        for (int c = cbegin; c < A.total_chunks; c += gstride) {
-            const int si = msys_of_chunk(A, c);
+        for (int u = cbegin; u < total_units; u += gstride) {
+            const int si = msys_of_chunk(A, u / MSUB);
             if (!inner_active(sst[si], sdc[si])) continue;
             const MSys &S = A.sys[si];
-            const int lc = c - S.chunk_begin;
-            const int r0 = lc * CH + lane;
+            const int lc = u - S.chunk_begin * MSUB;
+            const int r0 = lc * MUNIT + lane;
             float att = 0.0f, ats = 0.0f;
-#pragma unroll 2
-            for (int m = 0; m < RPL; ++m) {
+#pragma unroll
+            for (int m = 0; m < MRPL; ++m) {
                 const int row = r0 + m * LANES;
                 const float t = spmv_f32_row(S, row, S.z);
                 S.t[row] = t;
@@ -341,21 +345,21 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
         if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
             const MSys &S = A.sys[gi];
             double ftt, fts;
-            lanes_final_sum2(S.part, S.nchunks, lane, sm[gi], ftt, fts, gsync);
+            lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
             if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
         }
         __syncthreads();
         // x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
-        for (int c = cbegin; c < A.total_chunks; c += gstride) {
-            const int si = msys_of_chunk(A, c);
+        for (int u = cbegin; u < total_units; u += gstride) {
+            const int si = msys_of_chunk(A, u / MSUB);
             if (!inner_active(sst[si], sdc[si])) continue;
             const MSys &S = A.sys[si];
-            const int lc = c - S.chunk_begin;
-            const int r0 = lc * CH + lane;
+            const int lc = u - S.chunk_begin * MSUB;
+            const int r0 = lc * MUNIT + lane;
             const float alpha = (float)sst[si].alpha, w = (float)sst[si].w;
             float a0r = 0.0f, arr = 0.0f;
-#pragma unroll 2
-            for (int m = 0; m < RPL; ++m) {
+#pragma unroll
+            for (int m = 0; m < MRPL; ++m) {
                 const int row = r0 + m * LANES;
                 S.x[row] = __fmaf_rn(w, S.z[row], __fmaf_rn(alpha, S.y[row], S.x[row]));
                 const float r = __fmaf_rn(-w, S.t[row], S.s[row]);
@@ -367,13 +371,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, 1)
             }
             double t0r, trr;
             lanes_tree_sum2((double)a0r, (double)arr, lane, sm[gi], t0r, trr, gsync);
-            if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks)[lc] = make_double2(t0r, trr);
+            if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
             const MSys &S = A.sys[gi];
             double f0r, frr;
-            lanes_final_sum2(S.part + 2 * (size_t)S.nchunks, S.nchunks, lane, sm[gi], f0r, frr, gsync);
+            lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
             if (lane == 0) {
                 KState *st = &sst[gi];
                 st->rr = frr;
@@ -518,7 +522,7 @@ cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaS
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         g_m32_occ = occ;
     }
-    const int grid = std::max(1, std::min(A.total_chunks, device_sm_count() * occ));
+    const int grid = loop_grid(A.total_chunks * MSUB, MSUB, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     MSetArg a = A;

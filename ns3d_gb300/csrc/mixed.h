@@ -5,6 +5,12 @@
 
 namespace ns3d {
 
+// work unit of the FP32 loop kernel: MRPL rows per lane, MSUB units per chunk
+constexpr int MRPL = 2;
+constexpr int MUNIT = LANES * MRPL;
+constexpr int MSUB = CH / MUNIT;
+static_assert(PART_PER_CHUNK >= 5 * MSUB, "partials of the FP32 loop kernel");
+
 // FP64 defect-correction state of one system
 struct DCState {
     double rr, bb, tol, tol2, scale, error, tin, tin_min;

@@ -28,19 +28,31 @@ struct ApiError : std::runtime_error {
 };
 
 // owning device buffer
+// Device memory of the library: one stream-ordered pool per device, kept
+// reserved between solves (no cudaMalloc / cudaFree, which synchronize the
+// whole device and would stall every other solve running in the process).
+cudaMemPool_t device_pool();
+// bytes the pool holds reserved but unused (free for new solves)
+size_t pool_cached_bytes();
+
+// Device array allocated on a stream from the library pool and freed on the
+// same stream (stream-ordered: it may be released while work that uses it
+// is still queued on that stream).
 template <class T>
 struct DBuf {
     T *p = nullptr;
     size_t n = 0;
+    cudaStream_t st_ = nullptr;
     DBuf() = default;
     DBuf(const DBuf &) = delete;
     DBuf &operator=(const DBuf &) = delete;
     ~DBuf() { release(); }
-    void alloc(size_t count) {
+    void alloc(size_t count, cudaStream_t st) {
         release();
         n = count;
+        st_ = st;
         if (count == 0) return;
-        cudaError_t e = cudaMalloc((void **)&p, count * sizeof(T));
+        cudaError_t e = cudaMallocFromPoolAsync((void **)&p, count * sizeof(T), device_pool(), st);
         if (e != cudaSuccess) {
             p = nullptr;
             n = 0;
@@ -49,32 +61,28 @@ struct DBuf {
         }
     }
     void alloc_zero(size_t count, cudaStream_t st) {
-        alloc(count);
+        alloc(count, st);
         if (count) NS3D_CUDA_CHECK(cudaMemsetAsync(p, 0, count * sizeof(T), st));
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) cudaFreeAsync(p, st_);
         p = nullptr;
         n = 0;
     }
 };
 
-// pinned host buffer
+// Host staging array of the small per-solve state copies.  Pageable memory:
+// a device-to-host copy into it returns once the copy is done, and freeing
+// it does not synchronize the device (cudaFreeHost would).
 template <class T>
 struct HBuf {
+    std::vector<T> v;
     T *p = nullptr;
     size_t n = 0;
-    HBuf() = default;
-    HBuf(const HBuf &) = delete;
-    HBuf &operator=(const HBuf &) = delete;
-    ~HBuf() {
-        if (p) cudaFreeHost(p);
-    }
     void alloc(size_t count) {
-        if (p) cudaFreeHost(p);
-        p = nullptr;
+        v.assign(count, T());
+        p = count ? v.data() : nullptr;
         n = count;
-        if (count) NS3D_CUDA_CHECK(cudaMallocHost((void **)&p, count * sizeof(T)));
     }
 };
 
@@ -121,6 +129,18 @@ struct SolveOutcome {
     int iters = 0, info = 0, work = 0;
     double error = 0;
     bool valid = false;
+};
+
+// A CUDA stream destroyed after the buffers that are freed on it: declare it
+// before them in a class (members are destroyed in reverse order).
+struct OwnedStream {
+    cudaStream_t s = nullptr;
+    ~OwnedStream() {
+        if (s) {
+            cudaStreamSynchronize(s);
+            cudaStreamDestroy(s);
+        }
+    }
 };
 
 // A set of systems solved together by the batched BiCGSTAB kernels.

@@ -6,7 +6,8 @@
 // of concurrent solves overlap on the device.  The server admits queued
 // requests as soon as a slot is free and the device reports enough free
 // memory for the request's estimated footprint; finished solves release
-// their memory at once and the next requests are admitted -- continuous
+// their memory at once (stream-ordered, into the library's pool, without
+// synchronizing the device) and the next requests are admitted -- continuous
 // batching, not a queue in front of one solver.  Results do not depend on
 // what else runs: every kernel uses a fixed reduction order, so a solve gives
 // bit-identical fields alone and in the mix.
@@ -25,6 +26,10 @@
 #include <cuda_runtime.h>
 
 #include "../../include/ns3d_capi.h"
+
+namespace ns3d {
+size_t pool_cached_bytes();  // solver.cu: device memory the library pool holds free
+}
 
 namespace {
 
@@ -97,8 +102,14 @@ struct ns3d_server {
         size_t free_b = 0, total_b = 0;
         cudaSetDevice(device);
         if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return active == 0;
-        // keep 2 GiB of head room beyond the estimates of running solves
-        return j.bytes + (2ull << 30) <= free_b || active == 0;
+        // memory released by finished solves stays reserved in the library
+        // pool and counts as free here; keep 2 GiB of head room
+        size_t cached = 0;
+        try {
+            cached = ns3d::pool_cached_bytes();
+        } catch (...) {
+        }
+        return j.bytes + (2ull << 30) <= free_b + cached || active == 0;
     }
 
     void schedule_loop() {

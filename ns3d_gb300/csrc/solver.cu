@@ -33,19 +33,49 @@ void DevSys::allocate(int rows, int first_extent, cudaStream_t st) {
     d0 = first_extent;
     cell.alloc_zero(npad, st);
     coef.alloc_zero((size_t)7 * npad, st);
-    nbr.alloc(6 * (size_t)npad);
+    nbr.alloc(6 * (size_t)npad, st);
     NS3D_CUDA_CHECK(cudaMemsetAsync(nbr.p, 0xff, nbr.n * sizeof(int), st));
     rhs.alloc_zero(npad, st);
     rowsum.alloc_zero(npad, st);
     invdiag.alloc_zero(npad, st);
     DBuf<double> *ws[] = {&r, &r0, &p, &v, &y, &s, &z, &t};
     for (auto *b : ws) b->alloc_zero(npad, st);
-    part.alloc_zero((size_t)5 * std::max(nchunks, 1), st);
+    part.alloc_zero((size_t)PART_PER_CHUNK * std::max(nchunks, 1), st);
 }
 
 size_t DevSys::device_bytes() const {
     return cell.n * 4 + coef.n * 8 + nbr.n * 4 + (rhs.n + rowsum.n + invdiag.n) * 8 + 8 * (size_t)npad * 8 +
            part.n * 8;
+}
+
+cudaMemPool_t device_pool() {
+    static std::mutex mu;
+    static cudaMemPool_t pools[64] = {};
+    int dev = 0;
+    NS3D_CUDA_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= 64) throw ApiError(NS3D_ERR_CUDA, "device index out of range");
+    std::lock_guard<std::mutex> lk(mu);
+    if (!pools[dev]) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof props);
+        props.allocType = cudaMemAllocationTypePinned;
+        props.handleTypes = cudaMemHandleTypeNone;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = dev;
+        NS3D_CUDA_CHECK(cudaMemPoolCreate(&pools[dev], &props));
+        // keep released memory reserved for the next solves
+        uint64_t keep = UINT64_MAX;
+        NS3D_CUDA_CHECK(cudaMemPoolSetAttribute(pools[dev], cudaMemPoolAttrReleaseThreshold, &keep));
+    }
+    return pools[dev];
+}
+
+size_t pool_cached_bytes() {
+    cudaMemPool_t pool = device_pool();
+    uint64_t reserved = 0, used = 0;
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrReservedMemCurrent, &reserved);
+    cudaMemPoolGetAttribute(pool, cudaMemPoolAttrUsedMemCurrent, &used);
+    return reserved > used ? (size_t)(reserved - used) : 0;
 }
 
 void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
@@ -212,6 +242,7 @@ struct ns3d_handle {
     int rnx = 0, rny = 0, rnz = 0;  // raw image
     int nx = 0, ny = 0, nz = 0;     // solver frame
     int np = 0, nu = 0, nv = 0, nw = 0;
+    OwnedStream owned_stream;  // destroyed after every buffer freed on it
     cudaStream_t stream = nullptr;
 
     DBuf<uint8_t> img;
@@ -254,12 +285,6 @@ struct ns3d_handle {
         ph.dx = dx; ph.dy = dy; ph.dz = dz; ph.mu = mu; ph.rho = rho; ph.alpha = alpha; ph.beta = beta;
         ph.p0 = p0; ph.p1 = p1; ph.schemefactor = schemefactor;
         return ph;
-    }
-    ~ns3d_handle() {
-        if (stream) {
-            cudaStreamSynchronize(stream);
-            cudaStreamDestroy(stream);
-        }
     }
 
     // ---------------------------------------------------------------------
@@ -315,19 +340,19 @@ void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
     const long N = (long)nx * ny * nz, NU = (long)(nx + 1) * ny * nz;
     if (NU > 0x7fffffffL) throw ApiError(NS3D_ERR_ARG, "image too large for int32 indices");
     DBuf<uint8_t> draw;
-    draw.alloc((size_t)rx * ry * rz);
+    draw.alloc((size_t)rx * ry * rz, stream);
     NS3D_CUDA_CHECK(cudaMemcpyAsync(draw.p, raw, draw.n, cudaMemcpyHostToDevice, stream));
-    img.alloc(N);
+    img.alloc(N, stream);
     launch_build_image(draw.p, rx, ry, rz, prm.direction, std::max(prm.border, 0), prm.porevalue, img.p, nx, ny, nz,
                        stream);
-    pmap.alloc(N); vmap.alloc(N); wmap.alloc(N); umap.alloc(NU);
+    pmap.alloc(N, stream); vmap.alloc(N, stream); wmap.alloc(N, stream); umap.alloc(NU, stream);
     for (DBuf<int> *m : {&pmap, &vmap, &wmap, &umap}) NS3D_CUDA_CHECK(cudaMemsetAsync(m->p, 0xff, m->n * 4, stream));
     // cell tables sized by the worst case, shrunk after the counts are known
     DBuf<int> pcell, ucell, vcell, wcell;
-    pcell.alloc(N); ucell.alloc(NU); vcell.alloc(N); wcell.alloc(N);
+    pcell.alloc(N, stream); ucell.alloc(NU, stream); vcell.alloc(N, stream); wcell.alloc(N, stream);
     DBuf<int4> blk, tot;
-    blk.alloc(index_build_blocks(N));
-    tot.alloc(1);
+    blk.alloc(index_build_blocks(N), stream);
+    tot.alloc(1, stream);
     launch_index_build(img.p, nx, ny, nz, blk.p, tot.p, pmap.p, umap.p, vmap.p, wmap.p, pcell.p, ucell.p, vcell.p,
                        wcell.p, stream);
     int4 t;
@@ -611,7 +636,7 @@ void ns3d_handle::fields_to_image(const std::string &file) {
     if (have_out && write_fields) {
         const long N = (long)nx * ny * nz, NU = (long)(nx + 1) * ny * nz;
         DBuf<double> dimg;
-        dimg.alloc((size_t)std::max(3 * N, NU));
+        dimg.alloc((size_t)std::max(3 * N, NU), stream);
         std::vector<double> himg((size_t)std::max(3 * N, NU));
         std::string err, dir = std::to_string(prm.direction) + "-";
         auto dump = [&](const int *map, long cells, const double *f, int ex, const std::string &name) {
@@ -856,6 +881,7 @@ NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw, int32_t nx
     if (h.prm.dz <= 0) h.prm.dz = h.prm.dx;
     if (h.prm.porevalue != 0 && h.prm.porevalue != 1) h.prm.porevalue = 0;
     NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&h.stream, cudaStreamNonBlocking));
+    h.owned_stream.s = h.stream;
     h.build(raw, nx, ny, nz);
     h.dx = h.prm.dx; h.dy = h.prm.dy; h.dz = h.prm.dz; h.mu = h.prm.mu; h.rho = h.prm.rho;
     h.p0 = h.prm.p0; h.gradp = h.prm.gradp; h.border = h.prm.border; h.deltaRMR = h.prm.deltaRMR;
@@ -900,7 +926,7 @@ NS3D_API int ns3d_set_initial_fields(ns3d_handle *H, const double *pimg, const d
     h.default_fields();
     const long N = (long)h.nx * h.ny * h.nz, NU = (long)(h.nx + 1) * h.ny * h.nz;
     DBuf<double> tmp;
-    tmp.alloc((size_t)NU);
+    tmp.alloc((size_t)NU, h.stream);
     auto put = [&](const double *src, const int *map, long cells, double *f) {
         if (!src) return;
         NS3D_CUDA_CHECK(cudaMemcpyAsync(tmp.p, src, cells * 8, cudaMemcpyHostToDevice, h.stream));
@@ -946,7 +972,7 @@ NS3D_API int ns3d_get_field_images(ns3d_handle *H, double *pimg, double *uimg, d
     ns3d_handle &h = *checked(H);
     const long N = (long)h.nx * h.ny * h.nz, NU = (long)(h.nx + 1) * h.ny * h.nz;
     DBuf<double> tmp;
-    tmp.alloc((size_t)std::max(3 * N, NU));
+    tmp.alloc((size_t)std::max(3 * N, NU), h.stream);
     auto get = [&](double *dst, const int *map, long cells, const double *f) {
         if (!dst) return;
         launch_gather_image(map, cells, f, tmp.p, h.stream);
@@ -1004,6 +1030,8 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
     h.RMR = h.old_RMR = 0;
     h.kmom.reset_launch_count();
     h.kp.reset_launch_count();
+    // while several solves run at once the loop kernels take fewer SMs each
+    ActiveSolve active;
     if (h.prm.method == NS3D_SIMPLEC) h.run_simplec();
     else h.run_simpler_family(h.prm.method);
     return NS3D_OK;
