@@ -40,14 +40,18 @@ __device__ __forceinline__ double warp_tree_sum(double v) {
 // LANES threads, a named barrier when a larger block holds several groups of
 // LANES threads.  Returns the tree sum in lane 0 (other lanes get an
 // unspecified value).  `sm` needs LANES doubles.
-template <class Sync>
-__device__ __forceinline__ double lanes_tree_sum(double v, int lane, double *sm, Sync sync) {
-    v = warp_tree_sum(v);
+template <class T, class Sync>
+__device__ __forceinline__ T lanes_tree_sum(T v, int lane, T *sm, Sync sync) {
+    v = v + __shfl_down_sync(0xffffffffu, v, 16);
+    v = v + __shfl_down_sync(0xffffffffu, v, 8);
+    v = v + __shfl_down_sync(0xffffffffu, v, 4);
+    v = v + __shfl_down_sync(0xffffffffu, v, 2);
+    v = v + __shfl_down_sync(0xffffffffu, v, 1);
     if ((lane & 31) == 0) sm[lane >> 5] = v;
     sync();
-    double r = 0.0;
+    T r = T(0);
     if (lane < 32) {
-        r = (lane < LANES / 32) ? sm[lane] : 0.0;
+        r = (lane < LANES / 32) ? sm[lane] : T(0);
         for (int off = LANES / 64; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
     }
     sync();
@@ -58,15 +62,14 @@ __device__ __forceinline__ double lanes_tree_sum(double v, int lane, double *sm,
 // After the first level of a warp, lanes 0-15 carry the first sum and lanes
 // 16-31 the second, so every later level is one shuffle and one add for
 // both (FP64 issue is scarce on this GPU).  Results valid in lane 0.
-template <class Sync>
-__device__ __forceinline__ void lanes_tree_sum2(double a, double b, int lane, double *sm, double &ra, double &rb,
-                                                Sync sync) {
+template <class T, class Sync>
+__device__ __forceinline__ void lanes_tree_sum2(T a, T b, int lane, T *sm, T &ra, T &rb, Sync sync) {
     static_assert(2 * (LANES / 32) <= 32, "warp sums of both trees fit one warp");
-    ra = 0.0;
-    rb = 0.0;
+    ra = T(0);
+    rb = T(0);
     const bool lo = (lane & 16) == 0;
     // offset 16: lane l < 16 forms a_l + a_(l+16), lane l >= 16 forms b_(l-16) + b_l
-    double v = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
+    T v = (lo ? a : b) + __shfl_xor_sync(0xffffffffu, lo ? b : a, 16);
     v = v + __shfl_down_sync(0xffffffffu, v, 8);
     v = v + __shfl_down_sync(0xffffffffu, v, 4);
     v = v + __shfl_down_sync(0xffffffffu, v, 2);
@@ -76,9 +79,9 @@ __device__ __forceinline__ void lanes_tree_sum2(double a, double b, int lane, do
     if ((lane & 31) == 16) sm[NW + (lane >> 5)] = v;
     sync();
     if (lane < 32) {
-        double r = (lane < 2 * NW) ? sm[lane] : 0.0;
+        T r = (lane < 2 * NW) ? sm[lane] : T(0);
         for (int off = NW / 2; off >= 1; off >>= 1) r = r + __shfl_down_sync(0xffffffffu, r, off);
-        const double r2 = __shfl_sync(0xffffffffu, r, NW);
+        const T r2 = __shfl_sync(0xffffffffu, r, NW);
         ra = r;
         rb = r2;
     }
@@ -98,10 +101,10 @@ struct GroupSync {
 
 // Block of exactly LANES threads; the tree sum in thread 0.
 __device__ __forceinline__ double block_tree_sum(double v, double *sm) {
-    return lanes_tree_sum(v, threadIdx.x, sm, BlockSync());
+    return lanes_tree_sum<double>(v, threadIdx.x, sm, BlockSync());
 }
 __device__ __forceinline__ void block_tree_sum2(double a, double b, double *sm, double &ra, double &rb) {
-    lanes_tree_sum2(a, b, threadIdx.x, sm, ra, rb, BlockSync());
+    lanes_tree_sum2<double>(a, b, threadIdx.x, sm, ra, rb, BlockSync());
 }
 
 __device__ __forceinline__ double dmaxv(double a, double b) { return (b > a) ? b : a; }
@@ -133,7 +136,7 @@ __device__ __forceinline__ double lanes_final_sum(const double *part, int n, int
                                                   Sync sync) {
     double a = 0.0;
     for (int i = lane; i < n; i += LANES) a = a + __ldcg(part + (size_t)i * stride);
-    return lanes_tree_sum(a, lane, sm, sync);
+    return lanes_tree_sum<double>(a, lane, sm, sync);
 }
 // the same for the interleaved pairs part[2i] and part[2i+1] (16-byte aligned)
 template <class Sync>
@@ -145,7 +148,7 @@ __device__ __forceinline__ void lanes_final_sum2(const double *part, int n, int 
         a = a + q.x;
         b = b + q.y;
     }
-    lanes_tree_sum2(a, b, lane, sm, ra, rb, sync);
+    lanes_tree_sum2<double>(a, b, lane, sm, ra, rb, sync);
 }
 
 __device__ __forceinline__ double final_partials_sum(const double *part, int n, int stride, double *sm) {

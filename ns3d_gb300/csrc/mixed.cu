@@ -235,7 +235,8 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
 // ---- the FP32 inner iterations as one persistent cooperative kernel ----------
 // Same block shape, interleaving, partial regions and grid barrier as the
 // FP64 loop kernel (krylov.cu); its phases are those of the FP64 loop with
-// FP32 vectors, FP32 lane accumulation and FP64 trees and scalars.  The FP32
+// FP32 vectors and FP32 sums inside a work unit (FP32 pipe), FP64 sums of the
+// unit partials and FP64 scalars.  The FP32
 // results follow no fixed-order contract, so the work unit is a quarter
 // chunk (MUNIT = 256 rows, MRPL = 2 per lane): a group finishes a unit in one
 // round of loads, and a small system spreads over 4x more groups.  Every
@@ -293,8 +294,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 S.v[row] = v;
                 if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
             }
-            const double t = lanes_tree_sum((double)a, lane, sm[gi], gsync);
-            if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = t;
+            const float t = lanes_tree_sum<float>(a, lane, reinterpret_cast<float *>(sm[gi]), gsync);
+            if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
@@ -337,8 +338,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     ats = __fmaf_rn(t, S.s[row], ats);
                 }
             }
-            double tt, ts;
-            lanes_tree_sum2((double)att, (double)ats, lane, sm[gi], tt, ts, gsync);
+            float tt, ts;
+            lanes_tree_sum2<float>(att, ats, lane, reinterpret_cast<float *>(sm[gi]), tt, ts, gsync);
             if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
         }
         if (!grid_sync(bar, target, &s_ok)) break;
@@ -369,9 +370,10 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     arr = __fmaf_rn(r, r, arr);
                 }
             }
-            double t0r, trr;
-            lanes_tree_sum2((double)a0r, (double)arr, lane, sm[gi], t0r, trr, gsync);
-            if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
+            float t0r, trr;
+            lanes_tree_sum2<float>(a0r, arr, lane, reinterpret_cast<float *>(sm[gi]), t0r, trr, gsync);
+            if (lane == 0)
+                reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
         }
         if (!grid_sync(bar, target, &s_ok)) break;
         if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
