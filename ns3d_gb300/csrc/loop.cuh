@@ -27,13 +27,19 @@ __device__ __forceinline__ unsigned int ld_acquire(const unsigned int *p) {
     return v;
 }
 
+__device__ __forceinline__ void red_release_add(unsigned int *p, unsigned int v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The block barrier orders every thread's writes before thread 0's release
+// arrival; thread 0's acquire poll plus the closing block barrier order the
+// block's later reads after every other block's arrival.
 __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, int *s_ok) {
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
         target += gridDim.x;
-        __threadfence();  // the block's writes (ordered before by the block barrier) become visible
-        atomicAdd(&bar->count, 1u);
+        red_release_add(&bar->count, 1u);
         if ((int)(ld_acquire(&bar->count) - target) < 0) {
             const unsigned long long t0 = global_ns();
             unsigned int polls = 0;
@@ -45,7 +51,6 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, in
                 }
             }
         }
-        __threadfence();
         *s_ok = ok;
     }
     __syncthreads();

@@ -59,6 +59,25 @@ __device__ __forceinline__ float spmv_f32_row(const MSys &S, int row, const floa
     return acc;
 }
 
+// spmv_f32_row with the input vector given by a function of the column:
+// the loop kernel recomputes y = D^-1 p and z = D^-1 s of neighbouring rows
+// instead of waiting for their owners to store them
+template <class F>
+__device__ __forceinline__ float spmv_f32_fn(const MSys &S, int row, F xf) {
+    const size_t np = (size_t)S.npad;
+    const int *nb = S.nbr + row;
+    const float *cf = S.coef32 + row;
+    const int nW = nb[0 * np], nE = nb[1 * np], nS = nb[2 * np], nN = nb[3 * np], nB = nb[4 * np], nT = nb[5 * np];
+    float acc = cf[0] * xf(row);
+    acc = __fmaf_rn(cf[1 * np], xf(nW >= 0 ? nW : row), acc);
+    acc = __fmaf_rn(cf[3 * np], xf(nS >= 0 ? nS : row), acc);
+    acc = __fmaf_rn(cf[5 * np], xf(nB >= 0 ? nB : row), acc);
+    acc = __fmaf_rn(cf[6 * np], xf(nT >= 0 ? nT : row), acc);
+    acc = __fmaf_rn(cf[4 * np], xf(nN >= 0 ? nN : row), acc);
+    acc = __fmaf_rn(cf[2 * np], xf(nE >= 0 ? nE : row), acc);
+    return acc;
+}
+
 __device__ __forceinline__ double spmv_f64_row(const MSys &S, int row, const double *__restrict__ x) {
     const size_t np = (size_t)S.npad;
     const int *nb = S.nbr + row;
@@ -234,9 +253,14 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
 
 // ---- the FP32 inner iterations as one persistent cooperative kernel ----------
 // Same block shape, interleaving, partial regions and grid barrier as the
-// FP64 loop kernel (krylov.cu); its phases are those of the FP64 loop with
-// FP32 vectors and FP32 sums inside a work unit (FP32 pipe), FP64 sums of the
-// unit partials and FP64 scalars.  The FP32
+// FP64 loop kernel (krylov.cu), with FP32 vectors and FP32 sums inside a
+// work unit (FP32 pipe), FP64 sums of the unit partials and FP64 scalars.
+// FUSED: three phases and grid barriers per iteration instead of five: the
+// SpMV phases recompute y = D^-1 p and z = D^-1 s at neighbouring rows from
+// r, p, v (cheap in FP32) instead of waiting for a barrier after their owners
+// store them; p and v alternate between two buffers so that a phase never
+// overwrites what a neighbour still reads.  Otherwise the five phases of the
+// FP64 loop.  The FP32
 // results follow no fixed-order contract, so the work unit is a quarter
 // chunk (MUNIT = 256 rows, MRPL = 2 per lane): a group finishes a unit in one
 // round of loads, and a small system spreads over 4x more groups.  Every
@@ -244,6 +268,7 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
 // solve of the round is done or after `max_iters` iterations.
 __device__ __forceinline__ bool inner_active(const KState &k, int dc_done) { return !dc_done && !k.done; }
 
+template <bool FUSED>
 __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     k_m32_loop(const __grid_constant__ MSetArg A, GridBar *bar, int max_iters) {
     __shared__ KState sst[KMAX];
@@ -263,143 +288,268 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     __syncthreads();
     int it = 0;
     for (; it < max_iters; ++it) {
-        // p = r + beta (p - w v); y = D^-1 p
-        for (int u = cbegin; u < total_units; u += gstride) {
-            const int si = msys_of_chunk(A, u / MSUB);
-            if (!inner_active(sst[si], sdc[si])) continue;
-            const MSys &S = A.sys[si];
-            const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
-            const float beta = (float)sst[si].beta, w = (float)sst[si].w;
-#pragma unroll
-            for (int m = 0; m < MRPL; ++m) {
-                const int row = r0 + m * LANES;
-                const float p = __fmaf_rn(beta, __fmaf_rn(-w, S.v[row], S.p[row]), S.r[row]);
-                S.p[row] = p;
-                S.y[row] = S.invdiag32[row] * p;
+        if constexpr (FUSED) {
+            const bool odd = (it & 1) != 0;
+            // A: p' = r + beta (p - w v), y = D^-1 p' (stored for the own rows,
+            //    recomputed for neighbours); v' = A y, <r0, v'>.  p and v are read
+            //    from one buffer and written to the other.
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                const float beta = (float)sst[si].beta, w = (float)sst[si].w;
+                const float *pc = odd ? S.p2 : S.p, *vc = odd ? S.v2 : S.v;
+                float *pn = odd ? S.p : S.p2, *vn = odd ? S.v : S.v2;
+                auto yf = [&](int k) { return S.invdiag32[k] * __fmaf_rn(beta, __fmaf_rn(-w, vc[k], pc[k]), S.r[k]); };
+                float a = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float p = __fmaf_rn(beta, __fmaf_rn(-w, vc[row], pc[row]), S.r[row]);
+                    pn[row] = p;
+                    S.y[row] = S.invdiag32[row] * p;
+                    const float v = spmv_f32_fn(S, row, yf);
+                    vn[row] = v;
+                    if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
+                }
+                const float t = lanes_tree_sum<float>(a, lane, reinterpret_cast<float *>(sm[gi]), gsync);
+                if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
             }
-        }
-        if (!grid_sync(bar, target, &s_ok)) break;
-        // v = A y, <r0, v>
-        for (int u = cbegin; u < total_units; u += gstride) {
-            const int si = msys_of_chunk(A, u / MSUB);
-            if (!inner_active(sst[si], sdc[si])) continue;
-            const MSys &S = A.sys[si];
-            const int lc = u - S.chunk_begin * MSUB;
-            const int r0 = lc * MUNIT + lane;
-            float a = 0.0f;
-#pragma unroll
-            for (int m = 0; m < MRPL; ++m) {
-                const int row = r0 + m * LANES;
-                const float v = spmv_f32_row(S, row, S.y);
-                S.v[row] = v;
-                if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
+                if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
             }
-            const float t = lanes_tree_sum<float>(a, lane, reinterpret_cast<float *>(sm[gi]), gsync);
-            if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
-        }
-        if (!grid_sync(bar, target, &s_ok)) break;
-        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-            const MSys &S = A.sys[gi];
-            const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
-            if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
-        }
-        __syncthreads();
-        // s = r - alpha v; z = D^-1 s
-        for (int u = cbegin; u < total_units; u += gstride) {
-            const int si = msys_of_chunk(A, u / MSUB);
-            if (!inner_active(sst[si], sdc[si])) continue;
-            const MSys &S = A.sys[si];
-            const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
-            const float alpha = (float)sst[si].alpha;
-#pragma unroll
-            for (int m = 0; m < MRPL; ++m) {
-                const int row = r0 + m * LANES;
-                const float sv = __fmaf_rn(-alpha, S.v[row], S.r[row]);
-                S.s[row] = sv;
-                S.z[row] = S.invdiag32[row] * sv;
+            __syncthreads();
+            // B: s = r - alpha v', z = D^-1 s (stored for the own rows, recomputed
+            //    for neighbours); t = A z, <t, t>, <t, s>
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                const float alpha = (float)sst[si].alpha;
+                const float *vn = odd ? S.v : S.v2;
+                auto zf = [&](int k) { return S.invdiag32[k] * __fmaf_rn(-alpha, vn[k], S.r[k]); };
+                float att = 0.0f, ats = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float sv = __fmaf_rn(-alpha, vn[row], S.r[row]);
+                    S.s[row] = sv;
+                    S.z[row] = S.invdiag32[row] * sv;
+                    const float t = spmv_f32_fn(S, row, zf);
+                    S.t[row] = t;
+                    if (row < S.n) {
+                        att = __fmaf_rn(t, t, att);
+                        ats = __fmaf_rn(t, sv, ats);
+                    }
+                }
+                float tt, ts;
+                lanes_tree_sum2<float>(att, ats, lane, reinterpret_cast<float *>(sm[gi]), tt, ts, gsync);
+                if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
             }
-        }
-        if (!grid_sync(bar, target, &s_ok)) break;
-        // t = A z, <t, t>, <t, s>
-        for (int u = cbegin; u < total_units; u += gstride) {
-            const int si = msys_of_chunk(A, u / MSUB);
-            if (!inner_active(sst[si], sdc[si])) continue;
-            const MSys &S = A.sys[si];
-            const int lc = u - S.chunk_begin * MSUB;
-            const int r0 = lc * MUNIT + lane;
-            float att = 0.0f, ats = 0.0f;
-#pragma unroll
-            for (int m = 0; m < MRPL; ++m) {
-                const int row = r0 + m * LANES;
-                const float t = spmv_f32_row(S, row, S.z);
-                S.t[row] = t;
-                if (row < S.n) {
-                    att = __fmaf_rn(t, t, att);
-                    ats = __fmaf_rn(t, S.s[row], ats);
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                double ftt, fts;
+                lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
+                if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+            }
+            __syncthreads();
+            // C: x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                const float alpha = (float)sst[si].alpha, w = (float)sst[si].w;
+                float a0r = 0.0f, arr = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    S.x[row] = __fmaf_rn(w, S.z[row], __fmaf_rn(alpha, S.y[row], S.x[row]));
+                    const float r = __fmaf_rn(-w, S.t[row], S.s[row]);
+                    S.r[row] = r;
+                    if (row < S.n) {
+                        a0r = __fmaf_rn(S.r0[row], r, a0r);
+                        arr = __fmaf_rn(r, r, arr);
+                    }
+                }
+                float t0r, trr;
+                lanes_tree_sum2<float>(a0r, arr, lane, reinterpret_cast<float *>(sm[gi]), t0r, trr, gsync);
+                if (lane == 0)
+                    reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
+            }
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                double f0r, frr;
+                lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
+                if (lane == 0) {
+                    KState *st = &sst[gi];
+                    st->rr = frr;
+                    st->iter += 1;
+                    st->work += 1;
+                    const double eps2 = (double)FLT_EPSILON * FLT_EPSILON;
+                    if (!finite(frr) || !finite(st->alpha) || !finite(st->w)) {
+                        st->done = 1;
+                        st->info = 1;  // breakdown: the outer round discards this correction
+                    } else if (!(frr > st->tol2 && st->iter < st->maxit)) {
+                        st->done = 1;
+                    } else if (fabs(f0r) < eps2 * st->r0_sqnorm || st->w == 0.0) {
+                        st->done = 1;  // restart needed: end the round, the next one starts afresh
+                    } else {
+                        st->beta = (f0r / st->rho) * (st->alpha / st->w);
+                        st->rho = f0r;
+                    }
                 }
             }
-            float tt, ts;
-            lanes_tree_sum2<float>(att, ats, lane, reinterpret_cast<float *>(sm[gi]), tt, ts, gsync);
-            if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
-        }
-        if (!grid_sync(bar, target, &s_ok)) break;
-        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-            const MSys &S = A.sys[gi];
-            double ftt, fts;
-            lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
-            if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
-        }
-        __syncthreads();
-        // x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
-        for (int u = cbegin; u < total_units; u += gstride) {
-            const int si = msys_of_chunk(A, u / MSUB);
-            if (!inner_active(sst[si], sdc[si])) continue;
-            const MSys &S = A.sys[si];
-            const int lc = u - S.chunk_begin * MSUB;
-            const int r0 = lc * MUNIT + lane;
-            const float alpha = (float)sst[si].alpha, w = (float)sst[si].w;
-            float a0r = 0.0f, arr = 0.0f;
-#pragma unroll
-            for (int m = 0; m < MRPL; ++m) {
-                const int row = r0 + m * LANES;
-                S.x[row] = __fmaf_rn(w, S.z[row], __fmaf_rn(alpha, S.y[row], S.x[row]));
-                const float r = __fmaf_rn(-w, S.t[row], S.s[row]);
-                S.r[row] = r;
-                if (row < S.n) {
-                    a0r = __fmaf_rn(S.r0[row], r, a0r);
-                    arr = __fmaf_rn(r, r, arr);
+            __syncthreads();
+        } else {
+            // p = r + beta (p - w v); y = D^-1 p
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
+                const float beta = (float)sst[si].beta, w = (float)sst[si].w;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float p = __fmaf_rn(beta, __fmaf_rn(-w, S.v[row], S.p[row]), S.r[row]);
+                    S.p[row] = p;
+                    S.y[row] = S.invdiag32[row] * p;
                 }
             }
-            float t0r, trr;
-            lanes_tree_sum2<float>(a0r, arr, lane, reinterpret_cast<float *>(sm[gi]), t0r, trr, gsync);
-            if (lane == 0)
-                reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
-        }
-        if (!grid_sync(bar, target, &s_ok)) break;
-        if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-            const MSys &S = A.sys[gi];
-            double f0r, frr;
-            lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
-            if (lane == 0) {
-                KState *st = &sst[gi];
-                st->rr = frr;
-                st->iter += 1;
-                st->work += 1;
-                const double eps2 = (double)FLT_EPSILON * FLT_EPSILON;
-                if (!finite(frr) || !finite(st->alpha) || !finite(st->w)) {
-                    st->done = 1;
-                    st->info = 1;  // breakdown: the outer round discards this correction
-                } else if (!(frr > st->tol2 && st->iter < st->maxit)) {
-                    st->done = 1;
-                } else if (fabs(f0r) < eps2 * st->r0_sqnorm || st->w == 0.0) {
-                    st->done = 1;  // restart needed: end the round, the next one starts afresh
-                } else {
-                    st->beta = (f0r / st->rho) * (st->alpha / st->w);
-                    st->rho = f0r;
+            if (!grid_sync(bar, target, &s_ok)) break;
+            // v = A y, <r0, v>
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                float a = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float v = spmv_f32_row(S, row, S.y);
+                    S.v[row] = v;
+                    if (row < S.n) a = __fmaf_rn(S.r0[row], v, a);
+                }
+                const float t = lanes_tree_sum<float>(a, lane, reinterpret_cast<float *>(sm[gi]), gsync);
+                if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
+            }
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
+                if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+            }
+            __syncthreads();
+            // s = r - alpha v; z = D^-1 s
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int r0 = (u - S.chunk_begin * MSUB) * MUNIT + lane;
+                const float alpha = (float)sst[si].alpha;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float sv = __fmaf_rn(-alpha, S.v[row], S.r[row]);
+                    S.s[row] = sv;
+                    S.z[row] = S.invdiag32[row] * sv;
                 }
             }
+            if (!grid_sync(bar, target, &s_ok)) break;
+            // t = A z, <t, t>, <t, s>
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                float att = 0.0f, ats = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const float t = spmv_f32_row(S, row, S.z);
+                    S.t[row] = t;
+                    if (row < S.n) {
+                        att = __fmaf_rn(t, t, att);
+                        ats = __fmaf_rn(t, S.s[row], ats);
+                    }
+                }
+                float tt, ts;
+                lanes_tree_sum2<float>(att, ats, lane, reinterpret_cast<float *>(sm[gi]), tt, ts, gsync);
+                if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
+            }
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                double ftt, fts;
+                lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
+                if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+            }
+            __syncthreads();
+            // x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
+            for (int u = cbegin; u < total_units; u += gstride) {
+                const int si = msys_of_chunk(A, u / MSUB);
+                if (!inner_active(sst[si], sdc[si])) continue;
+                const MSys &S = A.sys[si];
+                const int lc = u - S.chunk_begin * MSUB;
+                const int r0 = lc * MUNIT + lane;
+                const float alpha = (float)sst[si].alpha, w = (float)sst[si].w;
+                float a0r = 0.0f, arr = 0.0f;
+    #pragma unroll
+                for (int m = 0; m < MRPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    S.x[row] = __fmaf_rn(w, S.z[row], __fmaf_rn(alpha, S.y[row], S.x[row]));
+                    const float r = __fmaf_rn(-w, S.t[row], S.s[row]);
+                    S.r[row] = r;
+                    if (row < S.n) {
+                        a0r = __fmaf_rn(S.r0[row], r, a0r);
+                        arr = __fmaf_rn(r, r, arr);
+                    }
+                }
+                float t0r, trr;
+                lanes_tree_sum2<float>(a0r, arr, lane, reinterpret_cast<float *>(sm[gi]), t0r, trr, gsync);
+                if (lane == 0)
+                    reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
+            }
+            if (!grid_sync(bar, target, &s_ok)) break;
+            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
+                const MSys &S = A.sys[gi];
+                double f0r, frr;
+                lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
+                if (lane == 0) {
+                    KState *st = &sst[gi];
+                    st->rr = frr;
+                    st->iter += 1;
+                    st->work += 1;
+                    const double eps2 = (double)FLT_EPSILON * FLT_EPSILON;
+                    if (!finite(frr) || !finite(st->alpha) || !finite(st->w)) {
+                        st->done = 1;
+                        st->info = 1;  // breakdown: the outer round discards this correction
+                    } else if (!(frr > st->tol2 && st->iter < st->maxit)) {
+                        st->done = 1;
+                    } else if (fabs(f0r) < eps2 * st->r0_sqnorm || st->w == 0.0) {
+                        st->done = 1;  // restart needed: end the round, the next one starts afresh
+                    } else {
+                        st->beta = (f0r / st->rho) * (st->alpha / st->w);
+                        st->rho = f0r;
+                    }
+                }
+            }
+            __syncthreads();
         }
-        __syncthreads();
         bool any = false;
         for (int q = 0; q < A.nsys; ++q) any = any || inner_active(sst[q], sdc[q]);
         if (!any) {
@@ -513,16 +663,25 @@ void launch_m32_init(const MSetArg &A, cudaStream_t st) {
 }
 
 
-static std::atomic<int> g_m32_occ{0};
+// Sets up to kFusedRows rows run the three-phase loop (fewer barriers; the
+// recomputed neighbour operands are cache hits); larger sets run the
+// five-phase loop, whose smaller working set stays in the L2 (measured: a
+// 42 K-row solve 9% faster fused, a 1 M-row solve 16% slower).
+constexpr long kFusedRows = 1L << 19;
+static std::atomic<int> g_m32_occ[2];
 
 cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaStream_t st) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
-    int occ = g_m32_occ.load();
+    long rows = 0;
+    for (int i = 0; i < A.nsys; ++i) rows += A.sys[i].n;
+    const bool fused = rows <= kFusedRows;
+    const void *fn = fused ? (const void *)k_m32_loop<true> : (const void *)k_m32_loop<false>;
+    int occ = g_m32_occ[fused].load();
     if (occ == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_m32_loop, LOOP_THREADS, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, LOOP_THREADS, 0);
         if (e != cudaSuccess) return e;
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
-        g_m32_occ = occ;
+        g_m32_occ[fused] = occ;
     }
     const int grid = loop_grid(A.total_chunks * MSUB, MSUB, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
@@ -530,7 +689,7 @@ cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaS
     MSetArg a = A;
     void *args[] = {&a, &bar, &max_iters};
     count_launches(1);
-    return cudaLaunchCooperativeKernel((const void *)k_m32_loop, grid, LOOP_THREADS, args, 0, st);
+    return cudaLaunchCooperativeKernel(fn, grid, LOOP_THREADS, args, 0, st);
 }
 
 void launch_dc_update(const MSetArg &A, cudaStream_t st) {

@@ -29,6 +29,7 @@ struct MSys {
     double *r64;           // FP64 residual
     const float *coef32, *invdiag32;
     float *x, *r, *r0, *p, *v, *y, *s, *z, *t;  // FP32 inner vectors (x is the correction)
+    float *p2, *v2;  // second buffers of p and v (the loop kernel alternates them)
     double *part;
     KState *st;  // inner BiCGSTAB state (scalars in FP64)
     DCState *dc;

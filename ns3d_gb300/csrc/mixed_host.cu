@@ -10,7 +10,7 @@ void DevSys::allocate_f32(cudaStream_t st) {
     if (coef32.n) return;
     coef32.alloc_zero((size_t)7 * npad, st);
     invdiag32.alloc_zero(npad, st);
-    for (DBuf<float> *b : {&fx, &fr, &fr0, &fp, &fv, &fy, &fs, &fz, &ft}) b->alloc_zero(npad, st);
+    for (DBuf<float> *b : {&fx, &fr, &fr0, &fp, &fv, &fy, &fs, &fz, &ft, &fp2, &fv2}) b->alloc_zero(npad, st);
 }
 
 void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
@@ -55,6 +55,7 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
         m.coef32 = S.coef32.p;
         m.invdiag32 = S.invdiag32.p;
         m.x = S.fx.p; m.r = S.fr.p; m.r0 = S.fr0.p; m.p = S.fp.p; m.v = S.fv.p;
+        m.p2 = S.fp2.p; m.v2 = S.fv2.p;
         m.y = S.fy.p; m.s = S.fs.p; m.z = S.fz.p; m.t = S.ft.p;
         m.part = S.part.p;
         m.st = st_.p + i;

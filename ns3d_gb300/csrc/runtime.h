@@ -98,7 +98,7 @@ struct DevSys {
     DBuf<double> r, r0, p, v, y, s, z, t, part;
     // FP32 copy of the system and the FP32 Krylov vectors (mixed precision),
     // allocated on first use
-    DBuf<float> coef32, invdiag32, fx, fr, fr0, fp, fv, fy, fs, fz, ft;
+    DBuf<float> coef32, invdiag32, fx, fr, fr0, fp, fv, fy, fs, fz, ft, fp2, fv2;
     void allocate(int rows, int first_extent, cudaStream_t st);
     void allocate_f32(cudaStream_t st);
     SysView view() const {

@@ -60,3 +60,25 @@ def test_mixed_linear_solve_reaches_fp64_tolerance(gpulib, oracle, sys):
     assert ig.info == capi.SUCCESS and io.info == capi.SUCCESS
     assert np.linalg.norm(_residual(coef, nbr, b, xg)) <= 1.0001 * tol * np.linalg.norm(b)
     assert rel_l2(xg, xo) <= 1e-6
+
+
+def test_mixed_linear_solve_large_set():
+    """A pressure system above 512K rows runs the five-phase FP32 loop (small
+    sets run the fused three-phase loop, covered above); it must meet the same
+    FP64 tolerance test."""
+    import ns3d_gb300
+    lib = ns3d_gb300.lib()
+    img, info = synth.random_fibres((96, 90, 80), 3, 0.85, seed=43)
+    g = solver(lib, img, params(lib, precision=capi.MIXED))
+    assert g.n(capi.SYS_P) > (1 << 19)
+    rng = np.random.default_rng(5)
+    n = g.sizes
+    g.set_fields(1.0 + 1e-3 * rng.standard_normal(n.np), 1e-6 * rng.standard_normal(n.nu),
+                 1e-6 * rng.standard_normal(n.nv), 1e-6 * rng.standard_normal(n.nw))
+    g.assemble_momentum()
+    g.assemble_pressure_correction(True)
+    tol = 1e-9
+    x, inf = g.solve_system(capi.SYS_P, np.zeros(g.n(capi.SYS_P)), tol, 4000)
+    coef, nbr, b, _ = g.system(capi.SYS_P)
+    assert inf.info == capi.SUCCESS
+    assert np.linalg.norm(_residual(coef, nbr, b, x)) <= 1.0001 * tol * np.linalg.norm(b)
