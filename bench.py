@@ -15,7 +15,7 @@ permeability solve; steps cycle through SIMPLEC, SIMPLER (N1=2), SIMPLERR
          the iterations of a solve: K1 p/y, K2 v = A y + <r0,v>, K3 s/z,
          K4 t = A z + <t,t>,<t,s>, K5 x/r + <r0,r>,<r,r>) of the
          pressure(-correction) solves: algorithmic bytes per row-iteration
-         (360 B: each vector element and matrix entry read or written once)
+         (408 B by the fixed (45s+48) formula; the fused phases touch 360 B)
          over the kernel's CUDA-event time
   cpu_baseline  the CPU oracle (the repo's restatement of the reference solver)
          on the first outer iterations of the same solve with every host core,
@@ -45,11 +45,13 @@ sys.path.insert(0, ROOT)
 METHODS = ["SIMPLEC", "SIMPLER", "SIMPLERR", "IDEAL"]
 SHAPE = (128, 128, 128)
 RADIUS, TARGET_PHI, SEED = 8, 0.5, 1
-# algorithmic bytes of one BiCGSTAB iteration per row: K1 48 (r, v, p, D^-1 in;
-# p, y out), K2 104 (7 coefficients, 6 indices, gathered y, r0 in; v out),
-# K3 40 (r, v, D^-1 in; s, z out), K4 104 (as K2 with z, s; t out), K5 64
-# (y, z, t, s, r0, x in; x, r out)
-LOOP_BYTES_PER_ROW = 360
+# algorithmic bytes of one FP64 BiCGSTAB iteration per row, by the fixed
+# formula (45s + 48) with s = 8: two SpMVs of (9s + 24) (7 coefficients, 6
+# indices, x in, y out), two Jacobi applications of 3s, 21s of vector
+# traffic.  The fused phases of the loop kernel touch 360 B (K1 48, K2 104,
+# K3 40, K4 104, K5 64: the Jacobi products ride in the p and s updates).
+LOOP_BYTES_PER_ROW = 408
+LOOP_FUSED_BYTES_PER_ROW = 360
 # FP64 instructions per row-iteration (a full 7-point row): two SpMVs (7 fma
 # each), five dot-product fma, vector updates p 2, y 1, s 1, z 1, x 2, r 1
 LOOP_FP64_PER_ROW = 27
@@ -334,7 +336,7 @@ def run_gpu(args):
     for m in METHODS:
         s = capi.Solver(lib, workload_params(capi, lib, m), raw, img.shape)
         solvers[m] = s
-    sizes = solvers["SIMPLEC"].sizes
+    sizes = solvers[METHODS[0]].sizes
 
     def step(i):
         s = solvers[METHODS[i % len(METHODS)]]
@@ -356,7 +358,7 @@ def run_gpu(args):
     value = world * args.steps / elapsed
     # per-kernel profile of the pressure(-correction) BiCGSTAB
     tot = {"ms": [0.0] * 6, "launches": [0] * 6, "rows": [0] * 6}
-    gpu_launches = int(solvers["SIMPLEC"].profile().total_launches)
+    gpu_launches = int(solvers[METHODS[0]].profile().total_launches)
     for s in solvers.values():
         p = s.profile()
         for k in range(6):
@@ -422,6 +424,8 @@ def run_gpu(args):
                              "traffic": None if traffic is None else traffic * loop_rows / max(loop_launches, 1),
                              "traffic_bytes_per_row_iteration": traffic,
                              "bytes_per_row_iteration": LOOP_BYTES_PER_ROW,
+                             "fused_bytes_per_row_iteration": LOOP_FUSED_BYTES_PER_ROW,
+                             "achieved_fused_bytes": achieved * LOOP_FUSED_BYTES_PER_ROW / LOOP_BYTES_PER_ROW,
                              "fp64_tflops": fp64_tflops, "fp64_peak_tflops": FP64_PEAK_TFLOPS,
                              "fp64_frac": fp64_tflops / FP64_PEAK_TFLOPS,
                              "avg_launch_ms": loop_ms / max(loop_launches, 1),

@@ -28,6 +28,9 @@ void launch_nbr_p(const Grid &g, const int *cell, int n, int npad, int *nbr, cud
 // physics.cu: assembly, corrections, diagnostics
 struct Phys {
     double dx, dy, dz, mu, rho, alpha, beta, p0, p1, schemefactor;
+    // 1/dx, 1/dy, 1/dz, 1/dx^2, 1/dy^2, 1/dz^2 computed once on the host
+    // (IEEE division is correctly rounded: the same bits as in the kernels)
+    double idx, idy, idz, idx2, idy2, idz2;
 };
 // momentum systems: coefficients, row sums and Jacobi inverse diagonal
 void launch_assemble_momentum(int comp, const Grid &g, const Phys &ph, const SysView &A, const double *uc,

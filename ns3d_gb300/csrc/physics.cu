@@ -34,8 +34,8 @@ __device__ __forceinline__ void finish_momentum_row(const SysView &A, int r, dou
 __global__ void k_mom_x(Grid g, Phys ph, SysView A, const double *__restrict__ uc, const double *__restrict__ vc,
                         const double *__restrict__ wc) {
     const double dx = ph.dx, dy = ph.dy, dz = ph.dz, mu = ph.mu, rho = ph.rho, sf = ph.schemefactor;
-    const double idx2 = 1 / (dx * dx), idy2 = 1 / (dy * dy), idz2 = 1 / (dz * dz);
-    const double idx = 1 / dx, idy = 1 / dy, idz = 1 / dz;
+    const double idx2 = ph.idx2, idy2 = ph.idy2, idz2 = ph.idz2;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     const int d0 = g.nx + 1, ny = g.ny, nz = g.nz;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
         int i, j, k;
@@ -165,8 +165,8 @@ __global__ void k_mom_x(Grid g, Phys ph, SysView A, const double *__restrict__ u
 __global__ void k_mom_y(Grid g, Phys ph, SysView A, const double *__restrict__ uc, const double *__restrict__ vc,
                         const double *__restrict__ wc) {
     const double dx = ph.dx, dy = ph.dy, dz = ph.dz, mu = ph.mu, rho = ph.rho, sf = ph.schemefactor;
-    const double idx2 = 1 / (dx * dx), idy2 = 1 / (dy * dy), idz2 = 1 / (dz * dz);
-    const double idx = 1 / dx, idy = 1 / dy, idz = 1 / dz;
+    const double idx2 = ph.idx2, idy2 = ph.idy2, idz2 = ph.idz2;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     const int d0 = g.nx, ny = g.ny, nz = g.nz;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
         int i, j, k;
@@ -296,8 +296,8 @@ __global__ void k_mom_y(Grid g, Phys ph, SysView A, const double *__restrict__ u
 __global__ void k_mom_z(Grid g, Phys ph, SysView A, const double *__restrict__ uc, const double *__restrict__ vc,
                         const double *__restrict__ wc) {
     const double dx = ph.dx, dy = ph.dy, dz = ph.dz, mu = ph.mu, rho = ph.rho, sf = ph.schemefactor;
-    const double idx2 = 1 / (dx * dx), idy2 = 1 / (dy * dy), idz2 = 1 / (dz * dz);
-    const double idx = 1 / dx, idy = 1 / dy, idz = 1 / dz;
+    const double idx2 = ph.idx2, idy2 = ph.idy2, idz2 = ph.idz2;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     const int d0 = g.nx, ny = g.ny, nz = g.nz;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
         int i, j, k;
@@ -424,7 +424,7 @@ __global__ void k_mom_z(Grid g, Phys ph, SysView A, const double *__restrict__ u
 // Assemble_RHS_u/v/w, src/NSBase.cxx:1445-1546
 template <int COMP>
 __global__ void k_mom_rhs(Grid g, Phys ph, SysView A, const double *__restrict__ p, const double *__restrict__ x) {
-    const double idx = 1 / ph.dx, idy = 1 / ph.dy, idz = 1 / ph.dz;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < A.n; r += gridDim.x * blockDim.x) {
         int i, j, k;
         g.ijk(A.cell[r], i, j, k);
@@ -467,7 +467,7 @@ __global__ void k_pressure(int mode, int relax, Grid g, Phys ph, SysView S, cons
                            const double *__restrict__ vc, const double *__restrict__ wc, const double *__restrict__ p) {
     const int nx = g.nx, ny = g.ny, nz = g.nz;
     const double dx2 = ph.dx * ph.dx, dy2 = ph.dy * ph.dy, dz2 = ph.dz * ph.dz;
-    const double idx = 1 / ph.dx, idy = 1 / ph.dy, idz = 1 / ph.dz;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < S.n; r += gridDim.x * blockDim.x) {
         int i, j, k;
         g.ijk(S.cell[r], i, j, k);
@@ -708,7 +708,7 @@ __global__ void k_divergence(Grid g, Phys ph, SysView P, const double *__restric
     __shared__ double sm[LANES];
     __shared__ bool last;
     const int nx = g.nx, ny = g.ny, nz = g.nz;
-    const double idx = 1 / ph.dx, idy = 1 / ph.dy, idz = 1 / ph.dz;
+    const double idx = ph.idx, idy = ph.idy, idz = ph.idz;
     for (int c = blockIdx.x; c < P.nchunks; c += gridDim.x) {
         double s2 = 0, sv = 0, mdv = 0, mdiv = 0;
         for (int m = 0; m < RPL; ++m) {

@@ -284,6 +284,8 @@ struct ns3d_handle {
         Phys ph;
         ph.dx = dx; ph.dy = dy; ph.dz = dz; ph.mu = mu; ph.rho = rho; ph.alpha = alpha; ph.beta = beta;
         ph.p0 = p0; ph.p1 = p1; ph.schemefactor = schemefactor;
+        ph.idx = 1 / dx; ph.idy = 1 / dy; ph.idz = 1 / dz;
+        ph.idx2 = 1 / (dx * dx); ph.idy2 = 1 / (dy * dy); ph.idz2 = 1 / (dz * dz);
         return ph;
     }
 
