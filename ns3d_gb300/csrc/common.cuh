@@ -131,11 +131,26 @@ __device__ __forceinline__ double block_tree_min(double v, double *sm) { return 
 // Final combination of `n` chunk partials (strided by `stride` doubles):
 // lane l sums partials l, l+LANES, ... in order, then the halving tree.
 // Result valid in lane 0.
+// The partials a lane adds are loaded 8 at a time before they are added (in
+// the same order), so the sum waits for one L2 round trip per 8 partials
+// instead of one per partial.
+constexpr int FINAL_BATCH = 8;
+
 template <class Sync>
 __device__ __forceinline__ double lanes_final_sum(const double *part, int n, int stride, int lane, double *sm,
                                                   Sync sync) {
     double a = 0.0;
-    for (int i = lane; i < n; i += LANES) a = a + __ldcg(part + (size_t)i * stride);
+    for (int base = lane; base < n; base += FINAL_BATCH * LANES) {
+        double v[FINAL_BATCH];
+#pragma unroll
+        for (int k = 0; k < FINAL_BATCH; ++k) {
+            const int i = base + k * LANES;
+            v[k] = (i < n) ? __ldcg(part + (size_t)i * stride) : 0.0;
+        }
+#pragma unroll
+        for (int k = 0; k < FINAL_BATCH; ++k)
+            if (base + k * LANES < n) a = a + v[k];
+    }
     return lanes_tree_sum<double>(a, lane, sm, sync);
 }
 // the same for the interleaved pairs part[2i] and part[2i+1] (16-byte aligned)
@@ -143,10 +158,19 @@ template <class Sync>
 __device__ __forceinline__ void lanes_final_sum2(const double *part, int n, int lane, double *sm, double &ra,
                                                  double &rb, Sync sync) {
     double a = 0.0, b = 0.0;
-    for (int i = lane; i < n; i += LANES) {
-        const double2 q = __ldcg(reinterpret_cast<const double2 *>(part) + i);
-        a = a + q.x;
-        b = b + q.y;
+    for (int base = lane; base < n; base += FINAL_BATCH * LANES) {
+        double2 v[FINAL_BATCH];
+#pragma unroll
+        for (int k = 0; k < FINAL_BATCH; ++k) {
+            const int i = base + k * LANES;
+            v[k] = (i < n) ? __ldcg(reinterpret_cast<const double2 *>(part) + i) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int k = 0; k < FINAL_BATCH; ++k)
+            if (base + k * LANES < n) {
+                a = a + v[k].x;
+                b = b + v[k].y;
+            }
     }
     lanes_tree_sum2<double>(a, b, lane, sm, ra, rb, sync);
 }
