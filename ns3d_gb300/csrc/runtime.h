@@ -173,7 +173,6 @@ class KrylovSet {
     DBuf<LoopProf> prof_;
     HBuf<int> h_err_;
     int nsys_ = 0, total_chunks_ = 0;
-    int prev_iters_ = 8;
     long launches_ = 0;
 };
 
@@ -203,7 +202,6 @@ class MixedSet {
     DBuf<GridBar> bar_;
     HBuf<int> h_err_;
     int nsys_ = 0, total_chunks_ = 0;
-    int prev_iters_ = 8;
 };
 
 }  // namespace ns3d

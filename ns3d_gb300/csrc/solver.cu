@@ -152,7 +152,7 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
     // iterations bound the whole solve.
     const long cap = 2L * maxit + 64;
     long issued = 0;
-    int max_iters = 0, loops = 0;
+    int loops = 0;
     std::vector<int> work_before(ns, 0);
     while (true) {
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
@@ -211,9 +211,7 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
         out[i].error = k.error;
         out[i].work = k.work;
         out[i].valid = true;
-        if (!k.zero_rhs) max_iters = std::max(max_iters, k.work);
     }
-    prev_iters_ = std::max(2, max_iters);
 }
 
 KrylovSet::~KrylovSet() {
