@@ -178,6 +178,13 @@ class KrylovSet {
 
 struct DCState;
 
+#ifndef NS3D_MIXED_INNER_TOL
+#define NS3D_MIXED_INNER_TOL 1e-4
+#endif
+#ifndef NS3D_MIXED_INNER_CAP
+#define NS3D_MIXED_INNER_CAP 400
+#endif
+
 // A set of systems solved by FP32 BiCGSTAB inside FP64 defect correction.
 // The FP32 copy of each matrix is refreshed from the FP64 one at every run.
 class MixedSet {
@@ -187,8 +194,8 @@ class MixedSet {
     // FP64 outcome of system i, mirrored into a KState (iter, info) for the
     // velocity post-processing kernel
     const KState *device_state(int i) const { return out_st_.p + i; }
-    double inner_rel_tol = 1e-4;  // floor of the per-round FP32 reduction target
-    int inner_cap = 400;          // FP32 iterations per round at most
+    double inner_rel_tol = NS3D_MIXED_INNER_TOL;  // floor of the per-round FP32 reduction target
+    int inner_cap = NS3D_MIXED_INNER_CAP;         // FP32 iterations per round at most
     ~MixedSet() = default;
 
   private:

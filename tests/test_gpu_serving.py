@@ -78,3 +78,18 @@ def test_batch_solve_matches_single_solves(gpulib):
         s = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
         assert s.solve().K == r.K
         s.close()
+
+
+def test_hbm_budget_limits_admission(gpulib):
+    """With an HBM budget below two requests' estimated footprint, the server
+    runs one solve at a time although four slots are free; every request
+    still completes."""
+    reqs = _requests(gpulib)[:3]
+    srv = capi.Server(gpulib, max_active=4, hbm_budget_bytes=1)
+    tickets = [srv.submit(p, synth.to_raw(img), img.shape) for p, img in reqs]
+    for t in tickets:
+        r, _ = srv.wait(t)
+        assert r.converged == 1 or r.iterations > 0
+    st = srv.stats()
+    srv.stop()
+    assert st.peak_active == 1 and st.completed == 3
