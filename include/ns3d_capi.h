@@ -266,6 +266,23 @@ NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t *nbr, const
                                    int32_t npad, double tol, int32_t maxit, void *stream, ns3d_solve_info *info);
 NS3D_API const char *ns3d_noalloc_last_error(void);
 
+/* ---- synthetic images on the device (no counterpart in the reference, which
+ * reads its geometry from .vti files, src/vtkio.cxx:96-150) ---------------- */
+/*
+ * Seeded porous image, nx*ny*nz uint8 in VTK order (x fastest; 1 = solid),
+ * written to `raw` (host, may be NULL).  kind 0: overlapping balls of integer
+ * radius with integer centres uniform in the box; kind 1: isotropic straight
+ * fibres (unions of balls of that radius centred at rint(p + t d), t = -L,
+ * -L+1, ... < L, L = box diagonal).  Primitives (from a splitmix64 stream of
+ * `seed`) are added in order until the solid fraction reaches 1 - porosity.
+ * *achieved = the resulting porosity; *nprims = primitives used; prims (may
+ * be NULL) receives up to max_prims of them, 6 doubles each (centre or point,
+ * then the unit direction of a fibre, zeros for a ball).
+ */
+NS3D_API int ns3d_generate_image(int32_t kind, int32_t nx, int32_t ny, int32_t nz, int32_t radius, double porosity,
+                                 uint64_t seed, uint8_t *raw, double *achieved, double *prims, int32_t max_prims,
+                                 int32_t *nprims);
+
 /* ---- many solves on one GPU (no counterpart in the reference, which runs
  * one image per process, src/navierstokes3D.cxx:516-542) ------------------- */
 /*

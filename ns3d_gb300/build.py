@@ -20,7 +20,7 @@ LIB = os.path.join(LIBDIR, "libns3d_gb300.so")
 EXE = os.path.join(LIBDIR, "NS3D")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-CU_FILES = ["geometry.cu", "physics.cu", "krylov.cu", "solver.cu", "noalloc.cu", "mixed.cu", "mixed_host.cu"]
+CU_FILES = ["geometry.cu", "physics.cu", "krylov.cu", "solver.cu", "noalloc.cu", "mixed.cu", "mixed_host.cu", "imagegen.cu"]
 CPP_FILES = ["hostio.cpp", "capi_host.cpp", "serving.cpp"]
 
 

@@ -334,3 +334,24 @@ class Server:
             self.stop()
         except Exception:
             pass
+
+
+def generate_image(lib, kind, shape, radius, porosity, seed, max_prims=1 << 16):
+    """ns3d_generate_image: a seeded sphere (kind 0) or fibre (kind 1) pack
+    rasterised on the device.  Returns (image in C order (x, y, z), achieved
+    porosity, primitives (k x 6))."""
+    f = lib.ns3d_generate_image
+    f.restype = C.c_int
+    f.argtypes = [C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_int32, C.c_double, C.c_uint64, _P(C.c_uint8),
+                  _P(C.c_double), _P(C.c_double), C.c_int32, _P(C.c_int32)]
+    nx, ny, nz = (int(v) for v in shape)
+    raw = np.empty(nx * ny * nz, np.uint8)
+    prims = np.empty((max_prims, 6), np.float64)
+    ach = C.c_double()
+    k = C.c_int32()
+    rc = f(int(kind), nx, ny, nz, int(radius), float(porosity), int(seed), _ptr(raw, C.c_uint8), C.byref(ach),
+           _ptr(prims, C.c_double), int(max_prims), C.byref(k))
+    if rc != 0:
+        raise NS3DError(rc, lib.ns3d_last_error().decode())
+    img = raw.reshape(nz, ny, nx).transpose(2, 1, 0).copy()
+    return img, ach.value, prims[:min(k.value, max_prims)].copy()

@@ -27,6 +27,9 @@ struct ApiError : std::runtime_error {
     ApiError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
 };
 
+// records the text ns3d_last_error() returns on this thread; returns code
+int report_error(int code, const std::string &m);
+
 // owning device buffer
 // Device memory of the library: one stream-ordered pool per device, kept
 // reserved between solves (no cudaMalloc / cudaFree, which synchronize the

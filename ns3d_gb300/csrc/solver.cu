@@ -227,6 +227,8 @@ static int set_error(int code, const std::string &m) {
     return code;
 }
 
+int report_error(int code, const std::string &m) { return set_error(code, m); }
+
 struct Scalars {
     double Q = 0, v_moy = 0, K = 0, normdiv = 0, reldiv = 0, velocityNorm = 0, maxdiv = 0, MaxDeltaV = 0;
 };
