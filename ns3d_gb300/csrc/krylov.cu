@@ -14,17 +14,17 @@
 // components, or the pressure system).  Their rows are processed as one list
 // of 1024-row chunks; the set is passed to every kernel by value
 // (__grid_constant__), so a block finds its system and the system's arrays
-// in constant memory and only reads the system's done flag from global
-// memory.  Finished systems make their chunks return at once; the block that
-// completes the last chunk of a system reduces that system's partials and
-// updates its scalars on the device.  One BiCGSTAB iteration is five kernels:
+// in constant memory.  One BiCGSTAB iteration has five phases:
 //   K1 p = r + beta (p - w v); y = D^-1 p
 //   K2 v = A y, <r0,v>                      -> alpha
 //   K3 s = r - alpha v; z = D^-1 s
 //   K4 t = A z, <t,t>, <t,s>                -> w
 //   K5 x += alpha y + w z; r = s - w t, <r0,r>, <r,r> -> convergence, beta
-// No kernel waits on another block: completion is detected with one atomic
-// counter per system, so every launch terminates on its own.
+// All iterations of a solve run in one persistent cooperative launch
+// (k_kr_loop), the phases separated by bounded grid barriers (loop.cuh).
+// The set-up (r = b - A x, norms) and the restart after |rho| breakdown are
+// separate launches whose last block to finish (one atomic counter per
+// system) combines the partials, so they wait on no other block.
 #include <atomic>
 #include <cfloat>
 

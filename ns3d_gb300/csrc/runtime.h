@@ -146,7 +146,7 @@ struct OwnedStream {
     }
 };
 
-// A set of systems solved together by the batched BiCGSTAB kernels.
+// A set of up to KMAX systems solved together by the BiCGSTAB loop kernel.
 class KrylovSet {
   public:
     void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out);

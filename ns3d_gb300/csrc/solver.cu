@@ -414,7 +414,7 @@ void ns3d_handle::log_solve(const char *comp, const SolveOutcome &o) {
 }
 
 // ComputeVelocityField, src/NSBase.cxx:1773-1884: the three components are
-// solved together by one batched BiCGSTAB launch sequence
+// solved together by one BiCGSTAB loop launch
 void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
     momentum_rhs();
     d2d(utemp.p, u.p, U.npad);
