@@ -291,6 +291,59 @@ def run_serving(capi, lib):
     }
 
 
+# Batch sample (opt-in, --batch): the configs[3] mix -- each edge drawn from
+# BATCH_EDGES per axis, a sphere pack (radius 3-8, porosity 0.35-0.9, overlap
+# allowed) or a fibre pack (radius 2-4, porosity 0.7-0.95), generated on the
+# device (ns3d_generate_image), flow along x, SIMPLEC -- solved by
+# ns3d_batch_solve in mixed precision and, as the reference point, by the
+# plain FP64 path one image at a time.
+BATCH_IMAGES = 16
+BATCH_EDGES = (32, 48, 64)
+
+
+def run_batch(capi, lib, n_images, edges, max_concurrent):
+    import ctypes as C
+    rng = np.random.default_rng(3)
+    imgs = []
+    for i in range(n_images):
+        shape = tuple(int(rng.choice(edges)) for _ in range(3))
+        if rng.integers(2) == 0:
+            kind, radius, phi = 0, int(rng.integers(3, 9)), float(rng.uniform(0.35, 0.9))
+        else:
+            kind, radius, phi = 1, int(rng.integers(2, 5)), float(rng.uniform(0.7, 0.95))
+        img, ach, _ = capi.generate_image(lib, kind, shape, radius, phi, 1000 + i)
+        imgs.append({"shape": shape, "raw": np.ascontiguousarray(img.transpose(2, 1, 0)).reshape(-1),
+                     "kind": kind, "phi": ach, "direction": 1, "method": 0})
+    k64, t64, cells = [], 0.0, 0
+    for r in imgs:
+        s = capi.Solver(lib, request_params(capi, lib, r, 0), r["raw"], r["shape"])
+        t = time.perf_counter()
+        res = s.solve()
+        t64 += time.perf_counter() - t
+        k64.append(res.K)
+        cells += s.sizes.np * (res.iterations + 1)
+        s.close()
+    lib = capi._declare_server(lib)
+    prm = (capi.Params * n_images)(*[request_params(capi, lib, r, 1) for r in imgs])
+    ptrs = (C.POINTER(C.c_uint8) * n_images)(*[r["raw"].ctypes.data_as(C.POINTER(C.c_uint8)) for r in imgs])
+    dims = np.array([d for r in imgs for d in r["shape"]], np.int32)
+    res = (capi.Result * n_images)()
+    status = np.zeros(n_images, np.int32)
+    t = time.perf_counter()
+    rc = lib.ns3d_batch_solve(prm, ptrs, dims.ctypes.data_as(C.POINTER(C.c_int32)), n_images, max_concurrent, res,
+                              status.ctypes.data_as(C.POINTER(C.c_int32)))
+    tb = time.perf_counter() - t
+    rel = [abs(r.K - k) / abs(k) for r, k in zip(res, k64)]
+    return {"workload": "%d images, edges from %s per axis, sphere (r 3-8, phi 0.35-0.9, overlapping) or fibre "
+                        "(r 2-4, phi 0.7-0.95) packs generated on the device, SIMPLEC, flow x" % (n_images, edges),
+            "status": int(rc),
+            "plain_fp64_one_at_a_time": {"solves_per_s": n_images / t64, "seconds": t64,
+                                         "cell_updates_per_s": cells / t64},
+            "batch_mixed": {"solves_per_s": n_images / tb, "seconds": tb, "max_concurrent": max_concurrent,
+                            "speedup_vs_plain_fp64": t64 / tb, "max_K_rel_err_vs_fp64": max(rel),
+                            "K_rel_err_vs_fp64": rel}}
+
+
 def run_reference(args):
     from ns3d_gb300 import capi
     world, rank, _, dist = dist_setup()
@@ -393,6 +446,10 @@ def run_gpu(args):
     serving = None
     if args.serving and world == 1:
         serving = run_serving(capi, lib)
+    batch = None
+    if args.batch and world == 1:
+        batch = run_batch(capi, lib, args.batch_images, tuple(int(x) for x in args.batch_edges.split(",")),
+                          SERVE_ACTIVE)
     line = None
     if rank == 0:
         cpu = None
@@ -437,6 +494,7 @@ def run_gpu(args):
                 "krylov_rows": kr_rows,
                 "cpu_baseline": cpu,
                 "serving": serving,
+                "batch": batch,
                 "clocks": clk}
         print(json.dumps(line))
     for s in solvers.values():
@@ -460,6 +518,9 @@ def main():
     ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
     ap.add_argument("--serving-edge", default="%d,%d" % SERVE_EDGE, help="min,max image edge of the requests")
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
+    ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
+    ap.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
+    ap.add_argument("--batch-edges", default=",".join(str(e) for e in BATCH_EDGES))
     ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
     ap.add_argument("--max-outer", type=int, default=2000,
