@@ -192,37 +192,36 @@ def cpu_sample(capi, img, method, outer):
     return dt, r.krylov_rows, r
 
 
-# Serving sample: a seeded stream of permeability requests (the serving
-# workload's mix, with edges bounded so the sample ends within about a
-# minute; --serving-requests and --serving-edge widen it):
-# image edges log-uniform in SERVE_EDGE, sphere packs (radius 3-8, porosity
-# 0.35-0.9) or fibre packs (radius 2-4, porosity 0.7-0.95), flow along x, y
-# or z, SIMPLEC or IDEAL, Poisson arrivals at SERVE_RATE requests/s.
-SERVE_REQUESTS = 12
-SERVE_EDGE = (32, 56)
-SERVE_RATE = 8.0
-SERVE_ACTIVE = 4
+# Serving sample: a seeded stream of permeability requests in the configs[4]
+# mix -- edges log-uniform in SERVE_EDGE (48-192 in configs[4]; bounded so a
+# request takes seconds, not minutes), a sphere pack (radius 3-8, porosity
+# 0.35-0.9) or a fibre pack (radius 2-4, porosity 0.7-0.95) generated on the
+# device, flow along x, y or z, SIMPLEC or IDEAL.  Throughput is counted in
+# equal windows of SERVE_WINDOW seconds: the plain FP64 path solves the stream
+# one request at a time; the server (mixed precision, up to SERVE_ACTIVE in
+# flight) receives Poisson arrivals at each rate of SERVE_RATES (a light load
+# for latency, a saturating one for capacity); requests still queued when the
+# window closes are dropped, those completed inside it are counted.  The
+# first SERVE_PREPARED requests of the stream are generated before the
+# windows start.
+SERVE_EDGE = (32, 48)
+SERVE_WINDOW = 30.0
+SERVE_PREPARED = 200  # requests generated before the windows
+SERVE_RATES = (1.0, 20.0)
+SERVE_ACTIVE = 8
 
 
-def serving_requests(capi, lib, n, seed=7):
-    from ns3d_gb300 import synth
-    rng = np.random.default_rng(seed)
-    reqs = []
-    for i in range(n):
-        shape = tuple(int(round(np.exp(rng.uniform(np.log(SERVE_EDGE[0]), np.log(SERVE_EDGE[1]))))) for _ in range(3))
-        if rng.integers(2) == 0:
-            img, info = synth.rsa_spheres(shape, int(rng.integers(3, 9)), float(rng.uniform(0.35, 0.9)), seed + 100 + i)
-            kind = "spheres"
-        else:
-            img, info = synth.random_fibres(shape, int(rng.integers(2, 5)), float(rng.uniform(0.7, 0.95)),
-                                            seed + 100 + i)
-            kind = "fibres"
-        direction = int(rng.integers(1, 4))
-        method = [0, 3][int(rng.integers(2))]  # SIMPLEC or IDEAL
-        reqs.append({"img": img, "raw": synth.to_raw(img), "shape": shape, "kind": kind, "phi": info["porosity"],
-                     "direction": direction, "method": method})
-    arrivals = np.cumsum(rng.exponential(1.0 / SERVE_RATE, size=n))
-    return reqs, arrivals - arrivals[0]
+def serving_request(capi, lib, i, seed=4):
+    rng = np.random.default_rng([seed, i])
+    shape = tuple(int(round(np.exp(rng.uniform(np.log(SERVE_EDGE[0]), np.log(SERVE_EDGE[1]))))) for _ in range(3))
+    if rng.integers(2) == 0:
+        kind, radius, phi = 0, int(rng.integers(3, 9)), float(rng.uniform(0.35, 0.9))
+    else:
+        kind, radius, phi = 1, int(rng.integers(2, 5)), float(rng.uniform(0.7, 0.95))
+    img, ach, _ = capi.generate_image(lib, kind, shape, radius, phi, seed * 1000003 + i)
+    return {"shape": shape, "raw": np.ascontiguousarray(img.transpose(2, 1, 0)).reshape(-1), "phi": ach,
+            "kind": "spheres" if kind == 0 else "fibres", "direction": int(rng.integers(1, 4)),
+            "method": [0, 3][int(rng.integers(2))]}
 
 
 def request_params(capi, lib, r, precision):
@@ -235,60 +234,74 @@ def request_params(capi, lib, r, precision):
 
 
 def run_serving(capi, lib):
-    """Plain FP64 one request at a time vs the continuous-batching server in
-    mixed precision (and in FP64) on the same request stream."""
-    reqs, arrivals = serving_requests(capi, lib, SERVE_REQUESTS)
-    # plain FP64, one at a time
-    k64, t64 = [], 0.0
-    for r in reqs:
+    """Windowed throughput: plain FP64 one request at a time vs the
+    continuous-batching server in mixed precision under Poisson arrivals."""
+    stream = [serving_request(capi, lib, i) for i in range(SERVE_PREPARED)]
+
+    def req(i):
+        return stream[i]
+
+    k64 = {}
+    t0 = time.perf_counter()
+    n_plain = 0
+    while time.perf_counter() - t0 < SERVE_WINDOW and n_plain < SERVE_PREPARED:
+        r = req(n_plain)
         s = capi.Solver(lib, request_params(capi, lib, r, 0), r["raw"], r["shape"])
-        t = time.perf_counter()
-        res = s.solve()
-        t64 += time.perf_counter() - t
-        k64.append(res.K)
+        k64[n_plain] = s.solve().K
         s.close()
-
-    def serve(precision):
+        n_plain += 1
+    plain_s = time.perf_counter() - t0
+    out = {"workload": "seeded request stream: edges log-uniform %d-%d, sphere (r 3-8, phi 0.35-0.9) or fibre "
+                       "(r 2-4, phi 0.7-0.95) packs generated on the device, flow x/y/z, SIMPLEC or IDEAL; "
+                       "windows of %.0f s" % (SERVE_EDGE[0], SERVE_EDGE[1], SERVE_WINDOW),
+           "plain_fp64_one_at_a_time": {"solves_per_s": n_plain / plain_s, "completed": n_plain,
+                                        "seconds": plain_s}}
+    for rate in SERVE_RATES:
+        rng = np.random.default_rng(int(rate * 1000))
         srv = capi.Server(lib, SERVE_ACTIVE)
+        subs = []
         t0 = time.perf_counter()
-        tickets = []
-        for r, a in zip(reqs, arrivals):
+        nxt, j = 0.0, 0
+        while True:
             now = time.perf_counter() - t0
-            if a > now:
-                time.sleep(a - now)
-            tickets.append(srv.submit(request_params(capi, lib, r, precision), r["raw"], r["shape"]))
-        ks, lats = [], []
-        for t in tickets:
+            if now >= SERVE_WINDOW:
+                break
+            if j >= SERVE_PREPARED:
+                break
+            if now >= nxt:
+                r = req(j)
+                ts = time.perf_counter() - t0
+                subs.append((j, srv.submit(request_params(capi, lib, r, 1), r["raw"], r["shape"]), ts))
+                j += 1
+                nxt += rng.exponential(1.0 / rate)
+            else:
+                time.sleep(min(nxt - now, SERVE_WINDOW - now))
+        srv.cancel_queued()
+        done = []
+        for i, t, ts in subs:
+            state, _, _ = srv.poll(t)
+            if state == 3:
+                continue
             res, lat = srv.wait(t)
-            ks.append(res.K)
-            lats.append(lat)
-        wall = time.perf_counter() - t0
-        st = srv.stats()
+            done.append((i, ts + lat, lat, res.K))
         srv.stop()
-        return ks, lats, wall, st
-
-    kmx, lmx, wmx, smx = serve(1)
-    kfp, lfp, wfp, sfp = serve(0)
-    rel = [abs(a - b) / abs(b) for a, b in zip(kmx, k64)]
-    rel_fp = [abs(a - b) / abs(b) for a, b in zip(kfp, k64)]
-    n = len(reqs)
-    cells = sum(int(np.prod(r["shape"])) for r in reqs)
-    return {
-        "workload": "%d seeded requests, edges log-uniform %d-%d, spheres (r 3-8, phi 0.35-0.9) or fibres "
-                    "(r 2-4, phi 0.7-0.95), flow x/y/z, SIMPLEC or IDEAL, Poisson arrivals %.1f/s, "
-                    "up to %d solves in flight" % (n, SERVE_EDGE[0], SERVE_EDGE[1], SERVE_RATE, SERVE_ACTIVE),
-        "voxels": cells,
-        "plain_fp64_one_at_a_time": {"solves_per_s": n / t64, "seconds": t64},
-        "served_mixed": {"solves_per_s": n / wmx, "seconds": wmx, "p50_latency_s": float(np.percentile(lmx, 50)),
-                         "p99_latency_s": float(np.percentile(lmx, 99)), "peak_active": smx.peak_active,
-                         "max_K_rel_err_vs_fp64": max(rel), "K_rel_err_vs_fp64": rel,
-                         "speedup_vs_plain_fp64": (n / wmx) / (n / t64)},
-        "served_fp64": {"solves_per_s": n / wfp, "seconds": wfp, "p50_latency_s": float(np.percentile(lfp, 50)),
-                        "p99_latency_s": float(np.percentile(lfp, 99)), "peak_active": sfp.peak_active,
-                        "max_K_rel_err_vs_fp64": max(rel_fp),
-                        "speedup_vs_plain_fp64": (n / wfp) / (n / t64)},
-        "note": "wall time of the served runs includes the Poisson arrival gaps (%.2f s spread)" % arrivals[-1],
-    }
+        inside = sorted((d for d in done if d[1] <= SERVE_WINDOW), key=lambda d: d[1])
+        lats = [d[2] for d in inside]
+        # completion rate once the first request is through (the window count
+        # also includes the initial ramp of a saturated server)
+        steady = (len(inside) - 1) / (inside[-1][1] - inside[0][1]) if len(inside) > 2 else None
+        errs = [abs(d[3] - k64[d[0]]) / abs(k64[d[0]]) for d in done if d[0] in k64]
+        out["served_mixed_rate_%g" % rate] = {
+            "arrival_rate_per_s": rate, "submitted": len(subs), "completed_in_window": len(inside),
+            "solves_per_s": len(inside) / SERVE_WINDOW,
+            "steady_solves_per_s": steady,
+            "steady_speedup_vs_plain_fp64": None if steady is None else steady / (n_plain / plain_s),
+            "p50_latency_s": float(np.percentile(lats, 50)) if lats else None,
+            "p99_latency_s": float(np.percentile(lats, 99)) if lats else None,
+            "speedup_vs_plain_fp64": (len(inside) / SERVE_WINDOW) / (n_plain / plain_s),
+            "K_compared": len(errs), "max_K_rel_err_vs_fp64": max(errs) if errs else None}
+    out["max_active"] = SERVE_ACTIVE
+    return out
 
 
 # Batch sample (opt-in, --batch): the configs[3] mix -- each edge drawn from
@@ -505,7 +518,7 @@ def run_gpu(args):
 
 
 def main():
-    global METHODS, MAX_OUTER, PRECISION, SERVE_REQUESTS, SERVE_EDGE, SERVE_ACTIVE
+    global METHODS, MAX_OUTER, PRECISION, SERVE_WINDOW, SERVE_EDGE, SERVE_ACTIVE
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -515,7 +528,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the end-to-end leg (profiling runs)")
     ap.add_argument("--no-serving", dest="serving", action="store_false",
                     help="skip the serving sample (plain FP64 one at a time vs the mixed-precision server)")
-    ap.add_argument("--serving-requests", type=int, default=SERVE_REQUESTS)
+    ap.add_argument("--serving-window", type=float, default=SERVE_WINDOW, help="seconds per throughput window")
     ap.add_argument("--serving-edge", default="%d,%d" % SERVE_EDGE, help="min,max image edge of the requests")
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
@@ -526,7 +539,7 @@ def main():
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
-    SERVE_REQUESTS = args.serving_requests
+    SERVE_WINDOW = args.serving_window
     SERVE_EDGE = tuple(int(x) for x in args.serving_edge.split(","))
     SERVE_ACTIVE = args.serving_active
     METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]

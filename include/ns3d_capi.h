@@ -318,6 +318,8 @@ NS3D_API int ns3d_server_poll(ns3d_server *s, int64_t ticket, int32_t *state, ns
 NS3D_API int ns3d_server_wait(ns3d_server *s, int64_t ticket, ns3d_result *result, double *latency_s);
 NS3D_API int ns3d_server_fields(ns3d_server *s, int64_t ticket, double *p, double *u, double *v, double *w);
 NS3D_API int ns3d_server_get_stats(ns3d_server *s, ns3d_server_stats *out);
+/* drops the requests not yet admitted (they end with NS3D_ERR_STATE) */
+NS3D_API int ns3d_server_cancel_queued(ns3d_server *s, int64_t *cancelled);
 /* finishes the queued and running requests, then frees the server */
 NS3D_API int ns3d_server_stop(ns3d_server *s);
 

@@ -266,6 +266,7 @@ def _declare_server(lib):
         "ns3d_server_fields": (C.c_int, [C.c_void_p, C.c_int64, _d, _d, _d, _d]),
         "ns3d_server_get_stats": (C.c_int, [C.c_void_p, _P(ServerStats)]),
         "ns3d_server_stop": (C.c_int, [C.c_void_p]),
+        "ns3d_server_cancel_queued": (C.c_int, [C.c_void_p, _P(C.c_int64)]),
         "ns3d_batch_solve": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32, _P(Result),
                                        _i32]),
     }
@@ -318,6 +319,11 @@ class Server:
         if rc != 0:
             raise NS3DError(rc, "fields of request %d unavailable" % ticket)
         return out
+
+    def cancel_queued(self):
+        n = C.c_int64()
+        self.lib.ns3d_server_cancel_queued(self.h, C.byref(n))
+        return n.value
 
     def stats(self):
         s = ServerStats()

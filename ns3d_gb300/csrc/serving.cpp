@@ -257,6 +257,22 @@ NS3D_API int ns3d_server_get_stats(ns3d_server *s, ns3d_server_stats *out) {
     return NS3D_OK;
 }
 
+NS3D_API int ns3d_server_cancel_queued(ns3d_server *s, int64_t *cancelled) {
+    if (!s) return NS3D_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    int64_t n = 0;
+    for (Job *j : s->queue) {
+        j->state = 3;
+        j->status = NS3D_ERR_STATE;
+        j->finished = Clock::now();
+        ++n;
+    }
+    s->queue.clear();
+    if (cancelled) *cancelled = n;
+    s->done_cv.notify_all();
+    return NS3D_OK;
+}
+
 NS3D_API int ns3d_server_stop(ns3d_server *s) {
     if (!s) return NS3D_ERR_ARG;
     {

@@ -93,3 +93,21 @@ def test_hbm_budget_limits_admission(gpulib):
     st = srv.stats()
     srv.stop()
     assert st.peak_active == 1 and st.completed == 3
+
+
+def test_cancel_queued_drops_only_waiting_requests(gpulib):
+    reqs = _requests(gpulib)[:4]
+    srv = capi.Server(gpulib, max_active=1)
+    tickets = [srv.submit(p, synth.to_raw(img), img.shape) for p, img in reqs]
+    import time
+    deadline = time.time() + 30
+    while srv.poll(tickets[0])[0] == 0 and time.time() < deadline:  # wait until the first is admitted
+        time.sleep(0.01)
+    n = srv.cancel_queued()
+    states = [srv.poll(t)[0] for t in tickets]
+    assert n >= 1 and states.count(3) == n
+    r, _ = srv.wait(tickets[0])
+    assert r.iterations > 0
+    st = srv.stats()
+    srv.stop()
+    assert st.completed + n == 4 or st.completed >= 1
