@@ -276,14 +276,16 @@ def run_serving(capi, lib):
                 nxt += rng.exponential(1.0 / rate)
             else:
                 time.sleep(min(nxt - now, SERVE_WINDOW - now))
-        srv.cancel_queued()
-        done = []
+        cancelled = srv.cancel_queued()
+        done, failed = [], 0
         for i, t, ts in subs:
-            state, _, _ = srv.poll(t)
-            if state == 3:
+            try:
+                res, lat = srv.wait(t)
+            except capi.NS3DError:
+                failed += 1  # cancelled while queued, or failed
                 continue
-            res, lat = srv.wait(t)
             done.append((i, ts + lat, lat, res.K))
+        failed -= cancelled
         srv.stop()
         inside = sorted((d for d in done if d[1] <= SERVE_WINDOW), key=lambda d: d[1])
         lats = [d[2] for d in inside]
@@ -293,6 +295,7 @@ def run_serving(capi, lib):
         errs = [abs(d[3] - k64[d[0]]) / abs(k64[d[0]]) for d in done if d[0] in k64]
         out["served_mixed_rate_%g" % rate] = {
             "arrival_rate_per_s": rate, "submitted": len(subs), "completed_in_window": len(inside),
+            "failed": failed, "cancelled_in_queue": cancelled,
             "solves_per_s": len(inside) / SERVE_WINDOW,
             "steady_solves_per_s": steady,
             "steady_speedup_vs_plain_fp64": None if steady is None else steady / (n_plain / plain_s),

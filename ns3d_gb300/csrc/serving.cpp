@@ -14,7 +14,9 @@
 #include <algorithm>
 #include <chrono>
 #include <condition_variable>
+#include <cstdio>
 #include <cstring>
+#include <string>
 #include <deque>
 #include <map>
 #include <memory>
@@ -55,6 +57,7 @@ struct Job {
     ns3d_result result;
     std::vector<double> fields[4];
     bool keep_fields = false;
+    std::string error;  // ns3d_last_error() of a failed request
     Clock::time_point submitted, started, finished;
 };
 
@@ -138,6 +141,11 @@ struct ns3d_server {
     void work(Job *j) {
         cudaSetDevice(device);
         int rc = run_one(*j);
+        if (rc != NS3D_OK) {
+            j->error = ns3d_last_error();  // the worker thread's error text
+            std::fprintf(stderr, "ns3d server: request %lld failed (%d): %s\n", (long long)j->ticket, rc,
+                         j->error.c_str());
+        }
         std::lock_guard<std::mutex> lk(mu);
         j->finished = Clock::now();
         j->status = rc;
