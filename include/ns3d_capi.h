@@ -197,6 +197,19 @@ NS3D_API int ns3d_set_output(ns3d_handle *h, const char *dir, const char *stem,
  * src/IDEAL.cxx:75-281) from the current initial fields.
  */
 NS3D_API int ns3d_solve(ns3d_handle *h);
+/*
+ * Pressure-drop sweep on one image (no counterpart in the reference, which
+ * solves one gradp per run; the Forchheimer analysis described in
+ * doc/NS3D_methods.tex needs several): for each gradp[i] the handle's p0/p1
+ * are re-derived (same rule as ns3d_open), the solve runs, and results[i]
+ * receives its result.  Geometry, index arrays and systems are built once.
+ * warm_start = 0: every solve starts from the default fields, so results[i]
+ * equals ns3d_open + ns3d_solve with that gradp; warm_start = 1: solve i > 0
+ * starts from solve i-1's fields scaled by gradp[i]/gradp[i-1] (exact for
+ * Stokes flow).  The fields of the last solve stay in the handle.
+ */
+NS3D_API int ns3d_solve_sweep(ns3d_handle *h, const double *gradp, int32_t n, int32_t warm_start,
+                              ns3d_result *results);
 NS3D_API int ns3d_get_result(const ns3d_handle *h, ns3d_result *r);
 
 /* ---- step-level entry points (one reference method each) --------------- */

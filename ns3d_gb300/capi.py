@@ -194,6 +194,16 @@ class Solver:
         self._check(self.lib.ns3d_solve(self.h))
         return self.result()
 
+    def sweep(self, gradps, warm_start=False):
+        """ns3d_solve_sweep: one solve per pressure gradient on this image."""
+        g = np.ascontiguousarray(gradps, dtype=np.float64)
+        res = (Result * len(g))()
+        f = self.lib.ns3d_solve_sweep
+        f.restype = C.c_int
+        f.argtypes = [C.c_void_p, _P(C.c_double), C.c_int32, C.c_int32, _P(Result)]
+        self._check(f(self.h, _ptr(g, C.c_double), len(g), int(bool(warm_start)), res))
+        return list(res)
+
     def result(self):
         r = Result()
         self._check(self.lib.ns3d_get_result(self.h, C.byref(r)))

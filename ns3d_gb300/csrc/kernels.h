@@ -53,6 +53,9 @@ void launch_correct_velocity(int comp, int simplec, const Grid &g, const Phys &p
 void launch_correct_velocity_simpler(int comp, const Grid &g, const Phys &ph, const SysView &A, const double *p,
                                      const double *hat, double *x, double p_0, double p_1, cudaStream_t st);
 // revert (iterations()==0 or failure) and optional per-node clamp
+// sweep warm start: u, v, w *= ratio; p = p0_new + (p - p0_old) ratio (padded arrays)
+void launch_scale_fields(double *u, int nu, double *v, int nv, double *w, int nw, double *p, int np, double ratio,
+                         double p0_old, double p0_new, cudaStream_t st);
 void launch_velocity_post(const double *temp, double *x, int n, const KState *st_dev, int limit, double dvmax,
                           cudaStream_t st);
 

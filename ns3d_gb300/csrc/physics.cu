@@ -878,6 +878,21 @@ __global__ void k_face_average(Grid g, const double *__restrict__ u, const doubl
     }
 }
 
+// warm start of a pressure-drop sweep: u, v, w *= ratio; p = p0' + (p - p0) ratio
+__global__ void k_scale_fields(double *u, int nu, double *v, int nv, double *w, int nw, double *p, int np,
+                               double ratio, double p0_old, double p0_new) {
+    const long total = (long)nu + nv + nw + np;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        if (i < nu) u[i] = u[i] * ratio;
+        else if (i < (long)nu + nv) v[i - nu] = v[i - nu] * ratio;
+        else if (i < (long)nu + nv + nw) w[i - nu - nv] = w[i - nu - nv] * ratio;
+        else {
+            const long k = i - nu - nv - nw;
+            p[k] = p0_new + (p[k] - p0_old) * ratio;
+        }
+    }
+}
+
 // ---- launchers ---------------------------------------------------------------
 static inline int rows_grid(long n) { return (int)std::max<long>(1, std::min<long>((n + 255) / 256, 152L * 16)); }
 static inline int chunk_grid(int nch) { return std::max(1, std::min(nch, 152 * 8)); }
@@ -929,6 +944,12 @@ void launch_correct_velocity_simpler(int comp, const Grid &g, const Phys &ph, co
     if (comp == 0) { count_launches(1); k_correct_simpler<0><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
     else if (comp == 1) { count_launches(1); k_correct_simpler<1><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
     else { count_launches(1); k_correct_simpler<2><<<rows_grid(A.n), 256, 0, st>>>(g, ph, A, p, hat, x, p_0, p_1); }
+}
+
+void launch_scale_fields(double *u, int nu, double *v, int nv, double *w, int nw, double *p, int np, double ratio,
+                         double p0_old, double p0_new, cudaStream_t st) {
+    count_launches(1);
+    k_scale_fields<<<152 * 8, 256, 0, st>>>(u, nu, v, nv, w, nw, p, np, ratio, p0_old, p0_new);
 }
 
 void launch_velocity_post(const double *temp, double *x, int n, const KState *st_dev, int limit, double dvmax,

@@ -292,6 +292,7 @@ struct ns3d_handle {
     // ---------------------------------------------------------------------
     void build(const uint8_t *raw, int rx, int ry, int rz);
     void default_fields();
+    void set_pressure_drop(double p0_in, double gradp_in);
     void assemble_all_momentum();
     void momentum_rhs();
     void compute_velocity_field(bool limit, double dvmax);
@@ -382,6 +383,18 @@ void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
     diag.alloc_zero(1, stream);
     h_diag.alloc(1);
     NS3D_CUDA_CHECK(cudaStreamSynchronize(stream));  // temporaries are freed on return
+}
+
+// p0, gradp and the outlet pressure p1 = p0 - gradp dx nx, shifted so that
+// p1 >= 0 (constructor, src/NSBase.cxx:155-161)
+void ns3d_handle::set_pressure_drop(double p0_in, double gradp_in) {
+    p0 = p0_in;
+    gradp = gradp_in;
+    p1 = -gradp * (dx * nx) + p0;
+    if (p1 < 0) {
+        p0 -= p1;
+        p1 = 0;
+    }
 }
 
 void ns3d_handle::default_fields() {
@@ -886,10 +899,9 @@ NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw, int32_t nx
     h.owned_stream.s = h.stream;
     h.build(raw, nx, ny, nz);
     h.dx = h.prm.dx; h.dy = h.prm.dy; h.dz = h.prm.dz; h.mu = h.prm.mu; h.rho = h.prm.rho;
-    h.p0 = h.prm.p0; h.gradp = h.prm.gradp; h.border = h.prm.border; h.deltaRMR = h.prm.deltaRMR;
+    h.border = h.prm.border; h.deltaRMR = h.prm.deltaRMR;
     // constructor constants, src/NSBase.cxx:155-179
-    h.p1 = -h.gradp * (h.dx * h.nx) + h.p0;
-    if (h.p1 < 0) { h.p0 -= h.p1; h.p1 = 0; }
+    h.set_pressure_drop(h.prm.p0, h.prm.gradp);
     h.schemefactor = 0; h.min_alpha = 0.001; h.min_beta = 0.001; h.relax = 0.05;
     h.speedup = h.relax * 0.5; h.maxconvdelta = 2.5;
     h.alpha = h.alpha0 = h.prm.alpha;
@@ -1036,6 +1048,33 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
     ActiveSolve active;
     if (h.prm.method == NS3D_SIMPLEC) h.run_simplec();
     else h.run_simpler_family(h.prm.method);
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_solve_sweep(ns3d_handle *H, const double *gradp, int32_t n, int32_t warm_start,
+                              ns3d_result *results) {
+    NS3D_TRY
+    ns3d_handle &h = *checked(H);
+    if (n < 0 || (n > 0 && (!gradp || !results))) throw ApiError(NS3D_ERR_ARG, "bad sweep arguments");
+    const double p0_user = h.prm.p0;
+    for (int i = 0; i < n; ++i) {
+        const double old_p0 = h.p0, old_gradp = h.gradp;
+        h.prm.gradp = gradp[i];
+        h.set_pressure_drop(p0_user, gradp[i]);
+        if (!warm_start || i == 0 || old_gradp == 0.0) {
+            h.default_fields();
+        } else {
+            // Stokes flow is linear in the pressure drop: scale the previous solution
+            const double ratio = gradp[i] / old_gradp;
+            launch_scale_fields(h.u.p, h.U.npad, h.v.p, h.V.npad, h.w.p, h.W.npad, h.p.p, h.P.npad, ratio, old_p0,
+                                h.p0, h.stream);
+            NS3D_CUDA_CHECK(cudaMemsetAsync(h.pc.p, 0, h.pc.n * 8, h.stream));
+        }
+        const int rc = ns3d_solve(H);
+        if (rc != NS3D_OK) return rc;
+        results[i] = h.res;
+    }
     return NS3D_OK;
     NS3D_CATCH
 }
