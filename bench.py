@@ -360,6 +360,36 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
                             "K_rel_err_vs_fp64": rel}}
 
 
+# Large sample (opt-in, --large): the configs[2] image -- 256^3 isotropic
+# straight fibres of radius 3, porosity ~0.85, seed 2, flow along z --
+# generated on the device; the first LARGE_OUTER outer SIMPLEC iterations in
+# plain FP64 and in mixed precision: time per outer iteration and the
+# FP32/FP64 time ratio (a converged 256^3 solve takes many minutes).
+LARGE_OUTER = 10
+
+
+def run_large(capi, lib, outer):
+    img, ach, _ = capi.generate_image(lib, 1, (256, 256, 256), 3, 0.85, 2)
+    raw = np.ascontiguousarray(img.transpose(2, 1, 0)).reshape(-1)
+    r = {"shape": (256, 256, 256), "direction": 3, "method": 0}
+    out = {"workload": "256^3 fibres r=3 phi=%.4f seed 2 (device generator), flow z, SIMPLEC, first %d outer "
+                       "iterations" % (ach, outer)}
+    for prec, name in ((0, "fp64"), (1, "mixed")):
+        p = request_params(capi, lib, r, prec)
+        p.maxitSIMPLE = outer
+        s = capi.Solver(lib, p, raw, img.shape)
+        t = time.perf_counter()
+        res = s.solve()
+        dt = time.perf_counter() - t
+        out[name] = {"seconds": dt, "seconds_per_outer_iteration": dt / max(res.iterations, 1),
+                     "outer_iterations": res.iterations, "K": res.K, "krylov_iterations": res.krylov_iterations,
+                     "np": s.sizes.np}
+        s.close()
+    out["fp32_fp64_time_ratio"] = out["mixed"]["seconds"] / out["fp64"]["seconds"]
+    out["K_rel_diff_at_this_iteration"] = abs(out["mixed"]["K"] - out["fp64"]["K"]) / abs(out["fp64"]["K"])
+    return out
+
+
 def run_reference(args):
     from ns3d_gb300 import capi
     world, rank, _, dist = dist_setup()
@@ -462,6 +492,7 @@ def run_gpu(args):
     serving = None
     if args.serving and world == 1:
         serving = run_serving(capi, lib)
+    large = run_large(capi, lib, args.large_outer) if (args.large and world == 1) else None
     batch = None
     if args.batch and world == 1:
         batch = run_batch(capi, lib, args.batch_images, tuple(int(x) for x in args.batch_edges.split(",")),
@@ -511,6 +542,7 @@ def run_gpu(args):
                 "cpu_baseline": cpu,
                 "serving": serving,
                 "batch": batch,
+                "large": large,
                 "clocks": clk}
         print(json.dumps(line))
     for s in solvers.values():
@@ -535,6 +567,8 @@ def main():
     ap.add_argument("--serving-edge", default="%d,%d" % SERVE_EDGE, help="min,max image edge of the requests")
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
+    ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
+    ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)
     ap.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
     ap.add_argument("--batch-edges", default=",".join(str(e) for e in BATCH_EDGES))
     ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
