@@ -209,6 +209,7 @@ SERVE_WINDOW = 30.0
 SERVE_PREPARED = 200  # requests generated before the windows
 SERVE_RATES = (1.0, 20.0)
 SERVE_ACTIVE = 8
+SERVE_PRECISION = 2  # mixed precision with the multilevel pressure preconditioner
 
 
 def serving_request(capi, lib, i, seed=4):
@@ -271,7 +272,7 @@ def run_serving(capi, lib):
             if now >= nxt:
                 r = req(j)
                 ts = time.perf_counter() - t0
-                subs.append((j, srv.submit(request_params(capi, lib, r, 1), r["raw"], r["shape"]), ts))
+                subs.append((j, srv.submit(request_params(capi, lib, r, SERVE_PRECISION), r["raw"], r["shape"]), ts))
                 j += 1
                 nxt += rng.exponential(1.0 / rate)
             else:
@@ -293,7 +294,7 @@ def run_serving(capi, lib):
         # also includes the initial ramp of a saturated server)
         steady = (len(inside) - 1) / (inside[-1][1] - inside[0][1]) if len(inside) > 2 else None
         errs = [abs(d[3] - k64[d[0]]) / abs(k64[d[0]]) for d in done if d[0] in k64]
-        out["served_mixed_rate_%g" % rate] = {
+        out["served_%s_rate_%g" % ("mixed_mg" if SERVE_PRECISION == 2 else "mixed", rate)] = {
             "arrival_rate_per_s": rate, "submitted": len(subs), "completed_in_window": len(inside),
             "failed": failed, "cancelled_in_queue": cancelled,
             "solves_per_s": len(inside) / SERVE_WINDOW,
@@ -340,7 +341,7 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
         cells += s.sizes.np * (res.iterations + 1)
         s.close()
     lib = capi._declare_server(lib)
-    prm = (capi.Params * n_images)(*[request_params(capi, lib, r, 1) for r in imgs])
+    prm = (capi.Params * n_images)(*[request_params(capi, lib, r, SERVE_PRECISION) for r in imgs])
     ptrs = (C.POINTER(C.c_uint8) * n_images)(*[r["raw"].ctypes.data_as(C.POINTER(C.c_uint8)) for r in imgs])
     dims = np.array([d for r in imgs for d in r["shape"]], np.int32)
     res = (capi.Result * n_images)()
@@ -374,7 +375,7 @@ def run_large(capi, lib, outer):
     r = {"shape": (256, 256, 256), "direction": 3, "method": 0}
     out = {"workload": "256^3 fibres r=3 phi=%.4f seed 2 (device generator), flow z, SIMPLEC, first %d outer "
                        "iterations" % (ach, outer)}
-    for prec, name in ((0, "fp64"), (1, "mixed")):
+    for prec, name in ((0, "fp64"), (1, "mixed"), (2, "mixed_mg")):
         p = request_params(capi, lib, r, prec)
         p.maxitSIMPLE = outer
         s = capi.Solver(lib, p, raw, img.shape)
@@ -386,7 +387,9 @@ def run_large(capi, lib, outer):
                      "np": s.sizes.np}
         s.close()
     out["fp32_fp64_time_ratio"] = out["mixed"]["seconds"] / out["fp64"]["seconds"]
+    out["mixed_mg_fp64_time_ratio"] = out["mixed_mg"]["seconds"] / out["fp64"]["seconds"]
     out["K_rel_diff_at_this_iteration"] = abs(out["mixed"]["K"] - out["fp64"]["K"]) / abs(out["fp64"]["K"])
+    out["K_rel_diff_mg_at_this_iteration"] = abs(out["mixed_mg"]["K"] - out["fp64"]["K"]) / abs(out["fp64"]["K"])
     return out
 
 
@@ -553,7 +556,7 @@ def run_gpu(args):
 
 
 def main():
-    global METHODS, MAX_OUTER, PRECISION, SERVE_WINDOW, SERVE_EDGE, SERVE_ACTIVE
+    global METHODS, MAX_OUTER, PRECISION, SERVE_WINDOW, SERVE_EDGE, SERVE_ACTIVE, SERVE_PRECISION
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -572,7 +575,9 @@ def main():
     ap.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
     ap.add_argument("--batch-edges", default=",".join(str(e) for e in BATCH_EDGES))
     ap.add_argument("--methods", default=",".join(METHODS), help="comma-separated subset of the four methods")
-    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_mg"])
+    ap.add_argument("--serving-precision", default="mixed_mg", choices=["mixed", "mixed_mg"],
+                    help="precision of the served solves")
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
@@ -581,7 +586,8 @@ def main():
     SERVE_ACTIVE = args.serving_active
     METHODS = [m.strip().upper() for m in args.methods.split(",") if m.strip()]
     MAX_OUTER = args.max_outer
-    PRECISION = 1 if args.precision == "mixed" else 0
+    PRECISION = {"fp64": 0, "mixed": 1, "mixed_mg": 2}[args.precision]
+    SERVE_PRECISION = 1 if args.serving_precision == "mixed" else 2
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -68,7 +68,9 @@ enum {
 enum { NS3D_SIMPLEC = 0, NS3D_SIMPLER = 1, NS3D_SIMPLERR = 2, NS3D_IDEAL = 3 };
 
 /* arithmetic of the inner solves */
-enum { NS3D_FP64 = 0, NS3D_MIXED = 1 };
+/* NS3D_MIXED_MG: as NS3D_MIXED, with an aggregation multilevel preconditioner
+ * (instead of Jacobi) in the FP32 pressure(-correction) solves */
+enum { NS3D_FP64 = 0, NS3D_MIXED = 1, NS3D_MIXED_MG = 2 };
 
 /* systems addressed by the step-level entry points */
 enum { NS3D_SYS_U = 0, NS3D_SYS_V = 1, NS3D_SYS_W = 2, NS3D_SYS_P = 3 };

@@ -14,7 +14,7 @@ NS3D_OK = 0
 SUCCESS, NUMERICAL_ISSUE, NO_CONVERGENCE, INVALID_INPUT = 0, 1, 2, 3
 ERR_ARG, ERR_OOM, ERR_CUDA, ERR_IO, ERR_PARSE, ERR_STATE, ERR_TIMEOUT, ERR_UNSUPPORTED = range(-1, -9, -1)
 SIMPLEC, SIMPLER, SIMPLERR, IDEAL = 0, 1, 2, 3
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_MG = 0, 1, 2
 SYS_U, SYS_V, SYS_W, SYS_P = 0, 1, 2, 3
 METHODS = {"SIMPLEC": SIMPLEC, "SIMPLER": SIMPLER, "SIMPLERR": SIMPLERR, "IDEAL": IDEAL}
 

@@ -17,7 +17,8 @@ namespace ns3d {
 // warn, a malformed value or a missing 'input' is fatal.  The key compared as
 // "deltaRMR" after lowercasing never matches (src/navierstokes3D.cxx:342), so
 // deltaRMR always keeps its default; that is reproduced.  One key is added:
-// precision = FP64 | MIXED selects the arithmetic of the inner solves.
+// precision = FP64 | MIXED | MIXED_MG selects the arithmetic (and, for
+// MIXED_MG, the preconditioner) of the inner solves.
 static std::string trim(const std::string &s) {
     const char *ws = " \t\r\n";
     size_t b = s.find_first_not_of(ws);
@@ -163,7 +164,8 @@ bool ini_read(const std::string &path, ns3d_params &p, IniFiles &files, std::str
     std::string pr = upper(precision);
     if (pr == "FP64") p.precision = NS3D_FP64;
     else if (pr == "MIXED") p.precision = NS3D_MIXED;
-    else return fatal("unknown precision '" + precision + "'. Valid values: FP64, MIXED");
+    else if (pr == "MIXED_MG") p.precision = NS3D_MIXED_MG;
+    else return fatal("unknown precision '" + precision + "'. Valid values: FP64, MIXED, MIXED_MG");
     if (p.dy <= 0.0) p.dy = p.dx;
     if (p.dz <= 0.0) p.dz = p.dx;
     return true;

@@ -39,7 +39,8 @@ static void usage() {
     printf("  direction      pressure gradient direction: 1=x, 2=y, 3=z\n");
     printf("  border         solid border thickness added along x (voxels)\n");
     printf("  method         algorithm: SIMPLEC, SIMPLER, SIMPLERR or IDEAL\n");
-    printf("  precision      inner-solve arithmetic: FP64 (default) or MIXED\n");
+    printf("  precision      inner-solve arithmetic: FP64 (default), MIXED, or MIXED_MG\n");
+    printf("                 (MIXED with a multilevel preconditioner in the pressure solves)\n");
 }
 
 int main(int argc, char **argv) {

@@ -251,6 +251,135 @@ __global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSet
     }
 }
 
+// ---- aggregation multilevel preconditioner (MIXED_MG) -------------------------
+struct MGView {
+    int n, npad;
+    const int *nbr;
+    const float *coef, *invdiag;
+    float *x, *b, *t;
+};
+
+// level k of the hierarchy of S (level 0: the FP32 system, solution x0 of
+// right-hand side b0, scratch S.t)
+__device__ __forceinline__ MGView mg_level(const MSys &S, int k, const float *b0, float *x0) {
+    MGView L;
+    if (k == 0) {
+        L.n = S.n;
+        L.npad = S.npad;
+        L.nbr = S.nbr;
+        L.coef = S.coef32;
+        L.invdiag = S.invdiag32;
+        L.x = x0;
+        L.b = const_cast<float *>(b0);
+        L.t = S.t;
+    } else {
+        const MGLevel &G = S.mg.lev[k];
+        L.n = G.n;
+        L.npad = G.npad;
+        L.nbr = G.nbr;
+        L.coef = G.coef;
+        L.invdiag = G.invdiag;
+        L.x = G.x;
+        L.b = G.b;
+        L.t = G.t;
+    }
+    return L;
+}
+
+// row of A x at one level (slot d+1 couples through neighbour d; a missing
+// neighbour has a zero coefficient and gathers the row itself)
+__device__ __forceinline__ float mg_spmv(const MGView &L, int row, const float *x) {
+    const size_t np = (size_t)L.npad;
+    const int *nb = L.nbr + row;
+    const float *cf = L.coef + row;
+    float acc = cf[0] * x[row];
+#pragma unroll
+    for (int d = 0; d < 6; ++d) {
+        const int c = nb[d * np];
+        acc = __fmaf_rn(cf[(d + 1) * np], x[c >= 0 ? c : row], acc);
+    }
+    return acc;
+}
+
+// x0 = M^-1 b0: one V-cycle -- a damped Jacobi sweep from zero, the residual
+// restricted to the next level (sum over the block), ... , Jacobi sweeps on
+// the coarsest level in block 0, then on the way up the correction of the
+// coarser level added and one damped Jacobi sweep.  Every thread of the grid
+// calls it (grid barriers between the passes); false when a barrier failed.
+__device__ bool mg_apply(const MSys &S, const float *b0, float *x0, GridBar *bar, unsigned int &target,
+                         int *s_ok) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int gth = gridDim.x * blockDim.x;
+    const int K = S.mg.nlev;
+    const float w = S.mg.omega;
+    for (int k = 0; k < K; ++k) {
+        const MGView L = mg_level(S, k, b0, x0);
+        const int lim = k == 0 ? L.npad : L.n;  // level 0: padding rows get finite values
+        for (int r = gtid; r < lim; r += gth) L.x[r] = w * L.invdiag[r] * L.b[r];
+        if (!grid_sync(bar, target, s_ok)) return false;
+        for (int r = gtid; r < L.n; r += gth) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+        if (!grid_sync(bar, target, s_ok)) return false;
+        const MGLevel &C = S.mg.lev[k + 1];
+        for (int I = gtid; I < C.n; I += gth) {
+            float acc = 0.0f;
+            for (int q = C.mstart[I]; q < C.mstart[I + 1]; ++q) acc += L.t[C.members[q]];
+            C.b[I] = acc;
+        }
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    {
+        const MGView L = mg_level(S, K, b0, x0);
+        if (blockIdx.x == 0) {
+            for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] = w * L.invdiag[r] * L.b[r];
+            __syncthreads();
+            for (int it = 0; it < S.mg.sweeps; ++it) {
+                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+                __syncthreads();
+                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] += w * L.invdiag[r] * L.t[r];
+                __syncthreads();
+            }
+        }
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    for (int k = K - 1; k >= 0; --k) {
+        const MGView L = mg_level(S, k, b0, x0);
+        const MGLevel &C = S.mg.lev[k + 1];
+        for (int r = gtid; r < L.n; r += gth) L.x[r] += C.x[C.agg[r]];
+        if (!grid_sync(bar, target, s_ok)) return false;
+        for (int r = gtid; r < L.n; r += gth) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+        if (!grid_sync(bar, target, s_ok)) return false;
+        for (int r = gtid; r < L.n; r += gth) L.x[r] += w * L.invdiag[r] * L.t[r];
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    return true;
+}
+
+// Galerkin operator of a coarse level: per row, the sum of its block's
+// diagonal and internal couplings, and per direction the couplings that
+// leave the block (in the members' order)
+__global__ void k_mg_galerkin(int npad_f, const int *__restrict__ nbr_f, const float *__restrict__ coef_f,
+                              MGLevel C) {
+    for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < C.n; I += gridDim.x * blockDim.x) {
+        float d = 0.0f, off[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        for (int q = C.mstart[I]; q < C.mstart[I + 1]; ++q) {
+            const int m = C.members[q];
+            d += coef_f[m];
+#pragma unroll
+            for (int dir = 0; dir < 6; ++dir) {
+                const int col = nbr_f[(size_t)dir * npad_f + m];
+                if (col < 0) continue;
+                const float a = coef_f[(size_t)(dir + 1) * npad_f + m];
+                if (C.agg[col] == I) d += a;
+                else off[dir] += a;
+            }
+        }
+        C.coef[I] = d;
+#pragma unroll
+        for (int dir = 0; dir < 6; ++dir) C.coef[(size_t)(dir + 1) * C.npad + I] = off[dir];
+        C.invdiag[I] = d != 0.0f ? 1.0f / d : 1.0f;
+    }
+}
+
 // ---- the FP32 inner iterations as one persistent cooperative kernel ----------
 // Same block shape, interleaving, partial regions and grid barrier as the
 // FP64 loop kernel (krylov.cu), with FP32 vectors and FP32 sums inside a
@@ -412,6 +541,9 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             }
             __syncthreads();
         } else {
+            // the preconditioner is multilevel for a single-system set with a
+            // hierarchy (uniform across the grid: the scalars are per-block copies)
+            const bool mg_on = A.nsys == 1 && A.sys[0].mg.nlev > 0 && inner_active(sst[0], sdc[0]);
             // p = r + beta (p - w v); y = D^-1 p
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -428,6 +560,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 }
             }
             if (!grid_sync(bar, target, &s_ok)) break;
+            // multilevel preconditioning: y = M^-1 p (replaces the Jacobi y)
+            if (mg_on && !mg_apply(A.sys[0], A.sys[0].p, A.sys[0].y, bar, target, &s_ok)) break;
             // v = A y, <r0, v>
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -469,6 +603,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 }
             }
             if (!grid_sync(bar, target, &s_ok)) break;
+            if (mg_on && !mg_apply(A.sys[0], A.sys[0].s, A.sys[0].z, bar, target, &s_ok)) break;
             // t = A z, <t, t>, <t, s>
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -625,6 +760,17 @@ __global__ void k_dc_update(const __grid_constant__ MSetArg A) {
 
 #undef NS3D_MCHUNK_LOOP
 
+void launch_mg_galerkin(const MSys &S, cudaStream_t st) {
+    for (int k = 1; k <= S.mg.nlev; ++k) {
+        const MGLevel &C = S.mg.lev[k];
+        const int npad_f = k == 1 ? S.npad : S.mg.lev[k - 1].npad;
+        const int *nbr_f = k == 1 ? S.nbr : S.mg.lev[k - 1].nbr;
+        const float *coef_f = k == 1 ? S.coef32 : S.mg.lev[k - 1].coef;
+        count_launches(1);
+        k_mg_galerkin<<<std::max(1, std::min((C.n + 255) / 256, 152 * 8)), 256, 0, st>>>(npad_f, nbr_f, coef_f, C);
+    }
+}
+
 // FP32 copy of a system's coefficients and inverse diagonal
 __global__ void k_to_f32(const double *__restrict__ coef, const double *__restrict__ invdiag, int npad,
                          float *__restrict__ coef32, float *__restrict__ invdiag32) {
@@ -673,8 +819,12 @@ static std::atomic<int> g_m32_occ[2];
 cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaStream_t st) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
     long rows = 0;
-    for (int i = 0; i < A.nsys; ++i) rows += A.sys[i].n;
-    const bool fused = rows <= kFusedRows;
+    bool mg = false;
+    for (int i = 0; i < A.nsys; ++i) {
+        rows += A.sys[i].n;
+        mg = mg || A.sys[i].mg.nlev > 0;
+    }
+    const bool fused = rows <= kFusedRows && !mg;  // the V-cycle runs in the five-phase loop
     const void *fn = fused ? (const void *)k_m32_loop<true> : (const void *)k_m32_loop<false>;
     int occ = g_m32_occ[fused].load();
     if (occ == 0) {

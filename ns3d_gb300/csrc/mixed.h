@@ -20,6 +20,30 @@ struct DCState {
     unsigned int counter, pad2_;
 };
 
+// Aggregation multilevel preconditioner of an FP32 inner solve (precision
+// mode MIXED_MG, single-system sets): level k+1 aggregates the rows of level
+// k by 2x2x2 blocks of their cells; its operator is the Galerkin product
+// (sum of the block's couplings; blocks couple through faces only, so it is
+// 7-point again, same slot order P,W,E,S,N,B,T).
+constexpr int MG_MAX = 6;
+struct MGLevel {
+    int n, npad;
+    const int *nbr;       // [6][npad], -1 none
+    float *coef;          // [7][npad]
+    float *invdiag;       // [npad]
+    const int *agg;       // [rows of level k-1]: the row of this level each belongs to
+    const int *mstart;    // [n + 1]: offsets into members
+    const int *members;   // rows of level k-1 of each row, ascending
+    float *x, *b, *t;     // V-cycle vectors [npad]
+};
+struct MGSet {
+    int nlev;             // coarse levels (0: Jacobi preconditioning)
+    int sweeps;           // Jacobi sweeps on the coarsest level
+    float omega;          // damping of the Jacobi smoother
+    int pad_;
+    MGLevel lev[MG_MAX + 1];  // lev[1..nlev]; lev[0] unused (the system itself)
+};
+
 struct MSys {
     int n, npad, nchunks, chunk_begin;
     const int *nbr;
@@ -33,6 +57,7 @@ struct MSys {
     double *part;
     KState *st;  // inner BiCGSTAB state (scalars in FP64)
     DCState *dc;
+    MGSet mg;
 };
 
 // A mixed solve set as a kernel argument (by value; systems in chunk order)
@@ -41,6 +66,8 @@ struct MSetArg {
     MSys sys[KMAX];
 };
 
+// Galerkin operators of every coarse level of `mg` from the FP32 system
+void launch_mg_galerkin(const MSys &sys, cudaStream_t st);
 void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
                    cudaStream_t st);
 void launch_dc_resid(const MSetArg &set, int first, cudaStream_t st);

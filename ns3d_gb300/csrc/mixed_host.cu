@@ -1,4 +1,5 @@
 // mixed_host.cu -- host driver of the mixed-precision solves (see mixed.cu).
+#include <algorithm>
 #include <cstring>
 
 #include "mixed.h"
@@ -11,6 +12,85 @@ void DevSys::allocate_f32(cudaStream_t st) {
     coef32.alloc_zero((size_t)7 * npad, st);
     invdiag32.alloc_zero(npad, st);
     for (DBuf<float> *b : {&fx, &fr, &fr0, &fp, &fv, &fy, &fs, &fz, &ft, &fp2, &fv2}) b->alloc_zero(npad, st);
+}
+
+// The aggregation hierarchy of system S from its cells: level k+1 groups
+// the rows of level k by the 2x2x2 block of their cell coordinates, until
+// a level has at most kMGCoarsest rows or MG_MAX levels exist.
+constexpr int kMGCoarsest = 512;
+
+static void build_mg(DevSys &S, cudaStream_t st) {
+    std::vector<int> cell((size_t)S.n);
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(cell.data(), S.cell.p, (size_t)S.n * 4, cudaMemcpyDeviceToHost, st));
+    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
+    std::vector<long long> ci(S.n), cj(S.n), ck(S.n);
+    for (int r = 0; r < S.n; ++r) {
+        const long long c = cell[r];
+        ck[r] = c % S.cell_nz;
+        cj[r] = (c / S.cell_nz) % S.cell_ny;
+        ci[r] = c / ((long long)S.cell_nz * S.cell_ny);
+    }
+    std::unique_ptr<MGHost> H(new MGHost());
+    int nf = S.n;
+    while (H->nlev < MG_MAX && nf > kMGCoarsest) {
+        // blocks of the current rows, numbered in ascending key order
+        std::vector<std::pair<long long, int>> key(nf);
+        for (int r = 0; r < nf; ++r) key[r] = {((ci[r] >> 1) << 42) | ((cj[r] >> 1) << 21) | (ck[r] >> 1), r};
+        std::sort(key.begin(), key.end());
+        std::vector<int> agg(nf);
+        std::vector<long long> bkey;
+        for (int q = 0; q < nf; ++q) {
+            if (q == 0 || key[q].first != key[q - 1].first) bkey.push_back(key[q].first);
+            agg[key[q].second] = (int)bkey.size() - 1;
+        }
+        const int nc = (int)bkey.size();
+        std::vector<int> mstart(nc + 1, 0), members(nf);
+        for (int r = 0; r < nf; ++r) mstart[agg[r] + 1]++;
+        for (int I = 0; I < nc; ++I) mstart[I + 1] += mstart[I];
+        std::vector<int> fill(mstart.begin(), mstart.end() - 1);
+        for (int r = 0; r < nf; ++r) members[fill[agg[r]]++] = r;  // ascending rows within a block
+        const int npad = (nc + 255) / 256 * 256;
+        std::vector<int> nbr((size_t)6 * npad, -1);
+        std::vector<long long> ni(nc), nj(nc), nk(nc);
+        for (int I = 0; I < nc; ++I) {
+            ni[I] = bkey[I] >> 42;
+            nj[I] = (bkey[I] >> 21) & ((1LL << 21) - 1);
+            nk[I] = bkey[I] & ((1LL << 21) - 1);
+        }
+        auto find = [&](long long a, long long b, long long c) -> int {
+            if (a < 0 || b < 0 || c < 0) return -1;
+            const long long k = (a << 42) | (b << 21) | c;
+            auto it = std::lower_bound(bkey.begin(), bkey.end(), k);
+            return (it != bkey.end() && *it == k) ? (int)(it - bkey.begin()) : -1;
+        };
+        for (int I = 0; I < nc; ++I) {  // directions W, E, S, N, B, T
+            nbr[(size_t)0 * npad + I] = find(ni[I] - 1, nj[I], nk[I]);
+            nbr[(size_t)1 * npad + I] = find(ni[I] + 1, nj[I], nk[I]);
+            nbr[(size_t)2 * npad + I] = find(ni[I], nj[I] - 1, nk[I]);
+            nbr[(size_t)3 * npad + I] = find(ni[I], nj[I] + 1, nk[I]);
+            nbr[(size_t)4 * npad + I] = find(ni[I], nj[I], nk[I] - 1);
+            nbr[(size_t)5 * npad + I] = find(ni[I], nj[I], nk[I] + 1);
+        }
+        MGHostLevel &L = H->lev[++H->nlev];
+        L.n = nc;
+        L.npad = npad;
+        L.nbr.alloc(nbr.size(), st);
+        L.agg.alloc(agg.size(), st);
+        L.mstart.alloc(mstart.size(), st);
+        L.members.alloc(members.size(), st);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(L.nbr.p, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, st));
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(L.agg.p, agg.data(), agg.size() * 4, cudaMemcpyHostToDevice, st));
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(L.mstart.p, mstart.data(), mstart.size() * 4, cudaMemcpyHostToDevice, st));
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(L.members.p, members.data(), members.size() * 4, cudaMemcpyHostToDevice, st));
+        L.coef.alloc_zero((size_t)7 * npad, st);
+        for (DBuf<float> *b : {&L.invdiag, &L.x, &L.b, &L.t}) b->alloc_zero(npad, st);
+        NS3D_CUDA_CHECK(cudaStreamSynchronize(st));  // the host vectors above are temporaries
+        ci = std::move(ni);
+        cj = std::move(nj);
+        ck = std::move(nk);
+        nf = nc;
+    }
+    S.mg = std::move(H);
 }
 
 void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
@@ -60,6 +140,27 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
         m.part = S.part.p;
         m.st = st_.p + i;
         m.dc = dc_.p + i;
+        if (use_mg && ns == 1 && S.n > kMGCoarsest && S.cell_ny > 0) {
+            if (!S.mg) build_mg(S, st);
+            m.mg.nlev = S.mg->nlev;
+            m.mg.sweeps = 30;
+            m.mg.omega = 0.6f;
+            for (int k = 1; k <= S.mg->nlev; ++k) {
+                MGHostLevel &H = S.mg->lev[k];
+                MGLevel &G = m.mg.lev[k];
+                G.n = H.n;
+                G.npad = H.npad;
+                G.nbr = H.nbr.p;
+                G.coef = H.coef.p;
+                G.invdiag = H.invdiag.p;
+                G.agg = H.agg.p;
+                G.mstart = H.mstart.p;
+                G.members = H.members.p;
+                G.x = H.x.p;
+                G.b = H.b.p;
+                G.t = H.t.p;
+            }
+        }
     }
     std::memset(&set_, 0, sizeof set_);
     set_.nsys = ns;
@@ -78,6 +179,7 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
     for (int i = 0; i < ns; ++i) {
         DevSys &S = *items[i].sys;
         launch_to_f32(S.coef.p, S.invdiag.p, S.npad, S.coef32.p, S.invdiag32.p, st);
+        if (set_.sys[i].mg.nlev > 0) launch_mg_galerkin(set_.sys[i], st);
         DCState d;
         std::memset(&d, 0, sizeof d);
         d.tol = items[i].tol;

@@ -3,6 +3,7 @@
 
 #include <cuda_runtime.h>
 
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -92,8 +93,21 @@ struct HBuf {
 inline int pad_rows(int n) { return ((n + CH - 1) / CH) * CH; }
 
 // one linear system (momentum component or pressure) and its Krylov workspace
+// Device arrays of the multilevel hierarchy of one system (MIXED_MG)
+struct MGHostLevel {
+    int n = 0, npad = 0;
+    DBuf<int> nbr, agg, mstart, members;
+    DBuf<float> coef, invdiag, x, b, t;
+};
+struct MGHost {
+    int nlev = 0;
+    MGHostLevel lev[MG_MAX + 1];
+};
+
 struct DevSys {
     int n = 0, npad = 0, nchunks = 0, d0 = 0;
+    int cell_ny = 0, cell_nz = 0;  // extents of the map behind `cell` (cell = (i ny + j) nz + k)
+    std::unique_ptr<MGHost> mg;    // built on first MIXED_MG use
     DBuf<int> cell;
     DBuf<double> coef;
     DBuf<int> nbr;
@@ -197,6 +211,7 @@ class MixedSet {
     // FP64 outcome of system i, mirrored into a KState (iter, info) for the
     // velocity post-processing kernel
     const KState *device_state(int i) const { return out_st_.p + i; }
+    bool use_mg = false;                          // multilevel preconditioner for single-system sets
     double inner_rel_tol = NS3D_MIXED_INNER_TOL;  // floor of the per-round FP32 reduction target
     int inner_cap = NS3D_MIXED_INNER_CAP;         // FP32 iterations per round at most
     ~MixedSet() = default;

@@ -255,7 +255,7 @@ struct ns3d_handle {
     HBuf<DiagOut> h_diag;
     KrylovSet kmom, kp;
     MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
-    bool mixed() const { return prm.precision == NS3D_MIXED; }
+    bool mixed() const { return prm.precision != NS3D_FP64; }
     void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
         if (mixed()) mp.run(items, stream, out);
         else kp.run(items, stream, out);
@@ -366,6 +366,8 @@ void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
     V.allocate(nv, nx, stream);
     W.allocate(nw, nx, stream);
     P.allocate(np, nx, stream);
+    P.cell_ny = ny;
+    P.cell_nz = nz;
     NS3D_CUDA_CHECK(cudaMemcpyAsync(U.cell.p, ucell.p, (size_t)nu * 4, cudaMemcpyDeviceToDevice, stream));
     NS3D_CUDA_CHECK(cudaMemcpyAsync(V.cell.p, vcell.p, (size_t)nv * 4, cudaMemcpyDeviceToDevice, stream));
     NS3D_CUDA_CHECK(cudaMemcpyAsync(W.cell.p, wcell.p, (size_t)nw * 4, cudaMemcpyDeviceToDevice, stream));
@@ -860,7 +862,8 @@ static void validate(const ns3d_params &p) {
     if (p.direction < 1 || p.direction > 3) throw ApiError(NS3D_ERR_ARG, "direction must be 1, 2 or 3");
     if (p.border < 0) throw ApiError(NS3D_ERR_ARG, "border must be >= 0");
     if (p.method < NS3D_SIMPLEC || p.method > NS3D_IDEAL) throw ApiError(NS3D_ERR_ARG, "unknown method");
-    if (p.precision != NS3D_FP64 && p.precision != NS3D_MIXED) throw ApiError(NS3D_ERR_ARG, "unknown precision");
+    if (p.precision != NS3D_FP64 && p.precision != NS3D_MIXED && p.precision != NS3D_MIXED_MG)
+        throw ApiError(NS3D_ERR_ARG, "unknown precision");
     if (p.N1 < 0 || p.N2 < 0) throw ApiError(NS3D_ERR_ARG, "N1 and N2 must be >= 0");
 }
 
@@ -902,6 +905,7 @@ NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw, int32_t nx
     h.border = h.prm.border; h.deltaRMR = h.prm.deltaRMR;
     // constructor constants, src/NSBase.cxx:155-179
     h.set_pressure_drop(h.prm.p0, h.prm.gradp);
+    h.mp.use_mg = h.prm.precision == NS3D_MIXED_MG;
     h.schemefactor = 0; h.min_alpha = 0.001; h.min_beta = 0.001; h.relax = 0.05;
     h.speedup = h.relax * 0.5; h.maxconvdelta = 2.5;
     h.alpha = h.alpha0 = h.prm.alpha;
@@ -1162,6 +1166,7 @@ NS3D_API int ns3d_solve_system(ns3d_handle *H, int32_t sys, const double *rhs, d
     std::vector<SolveOutcome> out;
     if (h.mixed()) {
         MixedSet ms;
+        ms.use_mg = h.prm.precision == NS3D_MIXED_MG;  // pressure systems (cell extents known) only
         ms.run({{&S, dx.p, b, tol, maxit}}, h.stream, out);
     } else {
         KrylovSet ks;

@@ -13,11 +13,12 @@ pytestmark = pytest.mark.gpu
 TOL_K_MIXED = 1e-4
 
 
+@pytest.mark.parametrize("precision", [capi.MIXED, capi.MIXED_MG])
 @pytest.mark.parametrize("method", ["SIMPLEC", "IDEAL"])
-def test_mixed_solve_matches_fp64_oracle(gpulib, oracle, method):
+def test_mixed_solve_matches_fp64_oracle(gpulib, oracle, method, precision):
     img, _ = synth.rsa_spheres((28, 20, 24), 3, 0.6, seed=41)
     kw = dict(method=method, maxitSIMPLE=400, simpletol=1e-6)
-    g = solver(gpulib, img, params(gpulib, precision=capi.MIXED, **kw))
+    g = solver(gpulib, img, params(gpulib, precision=precision, **kw))
     o = solver(oracle, img, params(oracle, **kw))
     rg, ro = g.solve(), o.solve()
     assert rg.converged == 1 and ro.converged == 1
@@ -35,13 +36,14 @@ def _residual(coef, nbr, b, x):
     return b - ax
 
 
-@pytest.mark.parametrize("sys", [capi.SYS_U, capi.SYS_P])
-def test_mixed_linear_solve_reaches_fp64_tolerance(gpulib, oracle, sys):
+@pytest.mark.parametrize("sys,precision", [(capi.SYS_U, capi.MIXED), (capi.SYS_P, capi.MIXED),
+                                           (capi.SYS_P, capi.MIXED_MG)])
+def test_mixed_linear_solve_reaches_fp64_tolerance(gpulib, oracle, sys, precision):
     """With precision = MIXED, ns3d_solve_system meets the FP64 test
     |b - A x| <= tol |b| (checked here in FP64 on the host) although the inner
     iterations run in FP32, and lands within tol of the FP64 oracle solution."""
     img, _ = synth.rsa_spheres((24, 18, 20), 3, 0.55, seed=42)
-    g = solver(gpulib, img, params(gpulib, precision=capi.MIXED))
+    g = solver(gpulib, img, params(gpulib, precision=precision))
     o = solver(oracle, img, params(oracle))
     rng = np.random.default_rng(4)
     n = g.sizes
@@ -65,20 +67,26 @@ def test_mixed_linear_solve_reaches_fp64_tolerance(gpulib, oracle, sys):
 def test_mixed_linear_solve_large_set():
     """A pressure system above 512K rows runs the five-phase FP32 loop (small
     sets run the fused three-phase loop, covered above); it must meet the same
-    FP64 tolerance test."""
+    FP64 tolerance test, with Jacobi and with the multilevel preconditioner,
+    and the multilevel one needs far fewer inner iterations."""
     import ns3d_gb300
     lib = ns3d_gb300.lib()
     img, info = synth.random_fibres((96, 90, 80), 3, 0.85, seed=43)
-    g = solver(lib, img, params(lib, precision=capi.MIXED))
-    assert g.n(capi.SYS_P) > (1 << 19)
-    rng = np.random.default_rng(5)
-    n = g.sizes
-    g.set_fields(1.0 + 1e-3 * rng.standard_normal(n.np), 1e-6 * rng.standard_normal(n.nu),
-                 1e-6 * rng.standard_normal(n.nv), 1e-6 * rng.standard_normal(n.nw))
-    g.assemble_momentum()
-    g.assemble_pressure_correction(True)
-    tol = 1e-9
-    x, inf = g.solve_system(capi.SYS_P, np.zeros(g.n(capi.SYS_P)), tol, 4000)
-    coef, nbr, b, _ = g.system(capi.SYS_P)
-    assert inf.info == capi.SUCCESS
-    assert np.linalg.norm(_residual(coef, nbr, b, x)) <= 1.0001 * tol * np.linalg.norm(b)
+    its = {}
+    for precision in (capi.MIXED, capi.MIXED_MG):
+        g = solver(lib, img, params(lib, precision=precision))
+        assert g.n(capi.SYS_P) > (1 << 19)
+        rng = np.random.default_rng(5)
+        n = g.sizes
+        g.set_fields(1.0 + 1e-3 * rng.standard_normal(n.np), 1e-6 * rng.standard_normal(n.nu),
+                     1e-6 * rng.standard_normal(n.nv), 1e-6 * rng.standard_normal(n.nw))
+        g.assemble_momentum()
+        g.assemble_pressure_correction(True)
+        tol = 1e-9
+        x, inf = g.solve_system(capi.SYS_P, np.zeros(g.n(capi.SYS_P)), tol, 4000)
+        coef, nbr, b, _ = g.system(capi.SYS_P)
+        assert inf.info == capi.SUCCESS
+        assert np.linalg.norm(_residual(coef, nbr, b, x)) <= 1.0001 * tol * np.linalg.norm(b)
+        its[precision] = inf.iterations
+        g.close()
+    assert its[capi.MIXED_MG] * 3 < its[capi.MIXED], its
