@@ -100,19 +100,19 @@ struct ns3d_server {
     bool any = false;
     int64_t completed = 0, failed = 0;
 
-    bool fits(const Job &j) {
-        if (hbm_budget) return reserved + j.bytes <= hbm_budget || active == 0;
+    // device memory available to a new solve: free memory plus what the
+    // library pool holds released by finished solves (queried without the
+    // server lock: the call can take a while when the device is busy)
+    size_t available_bytes() {
         size_t free_b = 0, total_b = 0;
         cudaSetDevice(device);
-        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return active == 0;
-        // memory released by finished solves stays reserved in the library
-        // pool and counts as free here; keep 2 GiB of head room
+        if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) return 0;
         size_t cached = 0;
         try {
             cached = ns3d::pool_cached_bytes();
         } catch (...) {
         }
-        return j.bytes + (2ull << 30) <= free_b + cached || active == 0;
+        return free_b + cached;
     }
 
     void schedule_loop() {
@@ -122,7 +122,18 @@ struct ns3d_server {
             if (stopping && queue.empty()) return;
             if (queue.empty() || active >= max_active) continue;
             Job *j = queue.front();
-            if (!fits(*j)) {  // wait for a running solve to release memory
+            bool ok;
+            if (hbm_budget) {
+                ok = reserved + j->bytes <= hbm_budget || active == 0;
+            } else {
+                lk.unlock();
+                const size_t avail = available_bytes();
+                lk.lock();
+                if (queue.empty() || queue.front() != j || active >= max_active) continue;  // changed meanwhile
+                // keep 2 GiB of head room beyond the estimates of running solves
+                ok = j->bytes + (2ull << 30) <= avail || active == 0;
+            }
+            if (!ok) {  // wait for a running solve to release memory
                 cv.wait_for(lk, std::chrono::milliseconds(5));
                 continue;
             }
