@@ -267,7 +267,8 @@ def run_serving(capi, lib):
             now = time.perf_counter() - t0
             if now >= SERVE_WINDOW:
                 break
-            if j >= SERVE_PREPARED:
+            if j >= SERVE_PREPARED:  # every prepared request submitted: serve until the window closes
+                time.sleep(max(0.0, SERVE_WINDOW - now))
                 break
             if now >= nxt:
                 r = req(j)
