@@ -428,6 +428,7 @@ def run_reference(args):
 
 
 def run_gpu(args):
+    global PRECISION
     import ns3d_gb300
     from ns3d_gb300 import capi, synth
     world, rank, local, dist = dist_setup()
@@ -493,6 +494,25 @@ def run_gpu(args):
         assert f[0].size == sizes.np
     e2e_elapsed = reduce_max(dist, time.perf_counter() - t1)
     e2e_value = world * e2e_steps / e2e_elapsed if e2e_steps else None
+    # the same workload in mixed precision with the multilevel pressure
+    # preconditioner: one solve per method, K against that method's FP64 solve
+    mixed_mg = None
+    if args.mixed_mg and world == 1:
+        saved, PRECISION = PRECISION, 2
+        t_mg, errs, its = 0.0, {}, {}
+        for m in METHODS:
+            s = capi.Solver(lib, workload_params(capi, lib, m), raw, img.shape)
+            t = time.perf_counter()
+            res = s.solve()
+            t_mg += time.perf_counter() - t
+            s.close()
+            its[m] = int(res.iterations)
+            if m in ks:
+                errs[m] = abs(res.K - ks[m]) / abs(ks[m])
+        PRECISION = saved
+        mixed_mg = {"solves_per_s": len(METHODS) / t_mg, "seconds_per_solve": t_mg / len(METHODS),
+                    "speedup_vs_plain_fp64": (len(METHODS) / t_mg) / value, "outer_iterations": its,
+                    "K_rel_err_vs_fp64": errs}
     serving = None
     if args.serving and world == 1:
         serving = run_serving(capi, lib)
@@ -544,6 +564,7 @@ def run_gpu(args):
                 "gpu_launches": gpu_launches,
                 "krylov_rows": kr_rows,
                 "cpu_baseline": cpu,
+                "mixed_mg": mixed_mg,
                 "serving": serving,
                 "batch": batch,
                 "large": large,
@@ -572,6 +593,8 @@ def main():
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
+    ap.add_argument("--no-mixed-mg", dest="mixed_mg", action="store_false",
+                    help="skip the workload's solves in mixed precision with the multilevel preconditioner")
     ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)
     ap.add_argument("--batch-images", type=int, default=BATCH_IMAGES)
     ap.add_argument("--batch-edges", default=",".join(str(e) for e in BATCH_EDGES))
