@@ -192,8 +192,8 @@ def cpu_sample(capi, img, method, outer):
     return dt, r.krylov_rows, r
 
 
-# Serving sample: a seeded stream of permeability requests in the configs[4]
-# mix -- edges log-uniform in SERVE_EDGE (48-192 in configs[4]; bounded so a
+# Serving sample: a seeded stream of mixed permeability requests -- edges
+# log-uniform in SERVE_EDGE (the serving mix spans 48-192; bounded here so a
 # request takes seconds, not minutes), a sphere pack (radius 3-8, porosity
 # 0.35-0.9) or a fibre pack (radius 2-4, porosity 0.7-0.95) generated on the
 # device, flow along x, y or z, SIMPLEC or IDEAL.  Throughput is counted in
@@ -309,7 +309,7 @@ def run_serving(capi, lib):
     return out
 
 
-# Batch sample (opt-in, --batch): the configs[3] mix -- each edge drawn from
+# Batch sample (opt-in, --batch): a mix of uneven images -- each edge drawn from
 # BATCH_EDGES per axis, a sphere pack (radius 3-8, porosity 0.35-0.9, overlap
 # allowed) or a fibre pack (radius 2-4, porosity 0.7-0.95), generated on the
 # device (ns3d_generate_image), flow along x, SIMPLEC -- solved by
@@ -362,7 +362,7 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
                             "K_rel_err_vs_fp64": rel}}
 
 
-# Large sample (opt-in, --large): the configs[2] image -- 256^3 isotropic
+# Large sample (opt-in, --large): a 256^3 image of isotropic
 # straight fibres of radius 3, porosity ~0.85, seed 2, flow along z --
 # generated on the device; the first LARGE_OUTER outer SIMPLEC iterations in
 # plain FP64 and in mixed precision: time per outer iteration and the

@@ -1,5 +1,5 @@
 """Mixed precision (FP32 BiCGSTAB inside FP64 defect correction) against the
-FP64 oracle.  Bar: |dK/K| <= 1e-4 (the benchmark spec's bar for the
+FP64 oracle.  Bar: |dK/K| <= 1e-4 (the stated tolerance of the
 mixed-precision results); the converged fields are also checked to 1e-5
 relative L2 and the outer-iteration count to within 10%."""
 import numpy as np
