@@ -362,6 +362,66 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
                             "K_rel_err_vs_fp64": rel}}
 
 
+# Merged sample (opt-in, --merged): the batch mix above in plain FP64 (SIMPLEC,
+# flow x), solved one image at a time, as a batch of concurrent solves on
+# their own streams (ns3d_batch_solve), and as a batch whose BiCGSTAB sets are
+# merged into shared persistent launches (ns3d_batch_solve_merged).  The three
+# legs follow the same trajectory bit for bit (fixed-order reductions), so
+# max_outer may cap the outer iterations of every leg alike.
+MERGED_IMAGES = 16
+
+
+def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
+    rng = np.random.default_rng(3)
+    imgs = []
+    for i in range(n_images):
+        shape = tuple(int(rng.choice(edges)) for _ in range(3))
+        if rng.integers(2) == 0:
+            kind, radius, phi = 0, int(rng.integers(3, 9)), float(rng.uniform(0.35, 0.9))
+        else:
+            kind, radius, phi = 1, int(rng.integers(2, 5)), float(rng.uniform(0.7, 0.95))
+        img, ach, _ = capi.generate_image(lib, kind, shape, radius, phi, 1000 + i)
+        imgs.append({"shape": shape, "raw": np.ascontiguousarray(img.transpose(2, 1, 0)).reshape(-1),
+                     "kind": kind, "phi": ach, "direction": 1, "method": 0})
+
+    def prm(r):
+        p = request_params(capi, lib, r, 0)
+        p.maxitSIMPLE = max_outer
+        return p
+
+    k1, t1, cells, rows = [], 0.0, 0, 0
+    for r in imgs:
+        s = capi.Solver(lib, prm(r), r["raw"], r["shape"])
+        t = time.perf_counter()
+        res = s.solve()
+        t1 += time.perf_counter() - t
+        k1.append(res.K)
+        cells += s.sizes.np * (res.iterations + 1)
+        rows += res.krylov_rows
+        s.close()
+    legs = {"plain_fp64_one_at_a_time": {"solves_per_s": n_images / t1, "seconds": t1,
+                                         "cell_updates_per_s": cells / t1,
+                                         "bicgstab_row_iterations_per_s": rows / t1}}
+    for name, merged in (("batch_fp64_streams", False), ("batch_fp64_merged", True)):
+        t = time.perf_counter()
+        res, status, g, rc = capi.batch_solve(lib, [prm(r) for r in imgs], [r["raw"] for r in imgs],
+                                              [r["shape"] for r in imgs], max_concurrent, merged=merged)
+        dt = time.perf_counter() - t
+        leg = {"solves_per_s": n_images / dt, "seconds": dt, "status": int(rc),
+               "speedup_vs_one_at_a_time": t1 / dt, "cell_updates_per_s": cells / dt,
+               "bicgstab_row_iterations_per_s": rows / dt,
+               "K_bit_identical_to_one_at_a_time": all(x.K == k for x, k in zip(res, k1)),
+               "max_concurrent": max_concurrent}
+        if g is not None:
+            leg["group"] = g.as_dict()
+            leg["mean_systems_per_set"] = g.systems / max(g.launches, 1)
+        legs[name] = leg
+    legs["workload"] = ("%d images, edges from %s per axis, sphere (r 3-8, phi 0.35-0.9, overlapping) or fibre "
+                        "(r 2-4, phi 0.7-0.95) packs generated on the device, SIMPLEC, flow x, plain FP64, "
+                        "at most %d outer iterations" % (n_images, edges, max_outer))
+    return legs
+
+
 # Large sample (opt-in, --large): a 256^3 image of isotropic
 # straight fibres of radius 3, porosity ~0.85, seed 2, flow along z --
 # generated on the device; the first LARGE_OUTER outer SIMPLEC iterations in
@@ -521,6 +581,10 @@ def run_gpu(args):
     if args.batch and world == 1:
         batch = run_batch(capi, lib, args.batch_images, tuple(int(x) for x in args.batch_edges.split(",")),
                           SERVE_ACTIVE)
+    merged = None
+    if args.merged and world == 1:
+        merged = run_merged(capi, lib, args.merged_images, tuple(int(x) for x in args.batch_edges.split(",")),
+                            SERVE_ACTIVE)
     line = None
     if rank == 0:
         cpu = None
@@ -567,6 +631,7 @@ def run_gpu(args):
                 "mixed_mg": mixed_mg,
                 "serving": serving,
                 "batch": batch,
+                "merged": merged,
                 "large": large,
                 "clocks": clk}
         print(json.dumps(line))
@@ -593,6 +658,9 @@ def main():
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
+    ap.add_argument("--merged", action="store_true",
+                    help="add the merged-solve-set sample (FP64 batch: one at a time, streams, merged)")
+    ap.add_argument("--merged-images", type=int, default=MERGED_IMAGES)
     ap.add_argument("--no-mixed-mg", dest="mixed_mg", action="store_false",
                     help="skip the workload's solves in mixed precision with the multilevel preconditioner")
     ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)

@@ -338,6 +338,38 @@ NS3D_API int ns3d_server_cancel_queued(ns3d_server *s, int64_t *cancelled);
 /* finishes the queued and running requests, then frees the server */
 NS3D_API int ns3d_server_stop(ns3d_server *s);
 
+/*
+ * Merged solve sets (no counterpart in the reference, which solves one image
+ * per process with Eigen, src/NSBase.cxx:1799,1825,1852,2343,2393,2397).
+ * Solver instances attached to one group pool their FP64 BiCGSTAB sets (the
+ * three momentum components, the pressure(-correction) system) while they
+ * solve: one persistent loop-kernel launch per round serves up to 64 systems
+ * of many images of different sizes, laid out as one ragged list of 1024-row
+ * chunks.  Every system keeps its own Krylov scalars and reduction order, so
+ * each result is bit-identical to the solve alone.  Mixed-precision solves
+ * ignore the group.  Attach with ns3d_set_group before ns3d_solve (NULL
+ * detaches); destroy a group only after every solve attached to it returned.
+ * The solves of a group must run on separate host threads.
+ */
+typedef struct ns3d_group ns3d_group;
+typedef struct ns3d_group_stats {
+    int64_t launches;  /* merged solve sets run */
+    int64_t requests;  /* member sets they served */
+    int64_t systems;   /* linear systems they solved */
+    int32_t max_systems, max_requests;  /* the largest merged set */
+} ns3d_group_stats;
+NS3D_API int ns3d_group_create(ns3d_group **out);
+NS3D_API int ns3d_set_group(ns3d_handle *h, ns3d_group *g);
+NS3D_API int ns3d_group_get_stats(ns3d_group *g, ns3d_group_stats *out);
+NS3D_API int ns3d_group_destroy(ns3d_group *g);
+/* every FP64 request of the server solves in one group (before the first submit) */
+NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t enable);
+NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out);
+/* ns3d_batch_solve with the FP64 solves merged; stats (may be NULL) of the group */
+NS3D_API int ns3d_batch_solve_merged(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                                     int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status,
+                                     ns3d_group_stats *stats);
+
 /* ---- host utilities (CUDA library only; no device work) ----------------- */
 /*
  * Parse an ini file like ReadInput (src/navierstokes3D.cxx:266-463): same

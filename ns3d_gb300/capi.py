@@ -264,6 +264,15 @@ class ServerStats(C.Structure):
         return {n: getattr(self, n) for n, _ in self._fields_}
 
 
+class GroupStats(C.Structure):
+    """ns3d_group_stats: merged solve sets run, member sets and systems served."""
+    _fields_ = [("launches", C.c_int64), ("requests", C.c_int64), ("systems", C.c_int64),
+                ("max_systems", C.c_int32), ("max_requests", C.c_int32)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 def _declare_server(lib):
     if getattr(lib, "_ns3d_server_declared", False):
         return lib
@@ -279,6 +288,14 @@ def _declare_server(lib):
         "ns3d_server_cancel_queued": (C.c_int, [C.c_void_p, _P(C.c_int64)]),
         "ns3d_batch_solve": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32, _P(Result),
                                        _i32]),
+        "ns3d_batch_solve_merged": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32,
+                                              _P(Result), _i32, _P(GroupStats)]),
+        "ns3d_server_set_merging": (C.c_int, [C.c_void_p, C.c_int32]),
+        "ns3d_server_group_stats": (C.c_int, [C.c_void_p, _P(GroupStats)]),
+        "ns3d_group_create": (C.c_int, [_P(C.c_void_p)]),
+        "ns3d_set_group": (C.c_int, [C.c_void_p, C.c_void_p]),
+        "ns3d_group_get_stats": (C.c_int, [C.c_void_p, _P(GroupStats)]),
+        "ns3d_group_destroy": (C.c_int, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -291,7 +308,7 @@ def _declare_server(lib):
 class Server:
     """Continuous-batching solve server (ns3d_server_*)."""
 
-    def __init__(self, lib, max_active, hbm_budget_bytes=0):
+    def __init__(self, lib, max_active, hbm_budget_bytes=0, merge=False):
         self.lib = _declare_server(lib)
         h = C.c_void_p()
         rc = self.lib.ns3d_server_start(int(max_active), int(hbm_budget_bytes), C.byref(h))
@@ -299,6 +316,15 @@ class Server:
             raise NS3DError(rc, "server start failed")
         self.h = h
         self.sizes = {}
+        if merge:
+            rc = self.lib.ns3d_server_set_merging(self.h, 1)
+            if rc != 0:
+                raise NS3DError(rc, "merging unavailable")
+
+    def group_stats(self):
+        g = GroupStats()
+        self.lib.ns3d_server_group_stats(self.h, C.byref(g))
+        return g
 
     def submit(self, params, raw_xfastest, dims, keep_fields=False):
         raw = np.ascontiguousarray(raw_xfastest, dtype=np.uint8).reshape(-1)
@@ -371,3 +397,53 @@ def generate_image(lib, kind, shape, radius, porosity, seed, max_prims=1 << 16):
         raise NS3DError(rc, lib.ns3d_last_error().decode())
     img = raw.reshape(nz, ny, nx).transpose(2, 1, 0).copy()
     return img, ach.value, prims[:min(k.value, max_prims)].copy()
+
+
+class Group:
+    """A solve group (ns3d_group_*): solver instances attached to it merge
+    their FP64 BiCGSTAB sets into shared persistent launches while they solve
+    on separate host threads."""
+
+    def __init__(self, lib):
+        self.lib = _declare_server(lib)
+        h = C.c_void_p()
+        rc = self.lib.ns3d_group_create(C.byref(h))
+        if rc != 0:
+            raise NS3DError(rc, lib.ns3d_last_error().decode())
+        self.h = h
+
+    def attach(self, solver):
+        rc = self.lib.ns3d_set_group(solver.h, self.h)
+        if rc != 0:
+            raise NS3DError(rc, self.lib.ns3d_last_error().decode())
+
+    def stats(self):
+        g = GroupStats()
+        self.lib.ns3d_group_get_stats(self.h, C.byref(g))
+        return g
+
+    def destroy(self):
+        if getattr(self, "h", None):
+            self.lib.ns3d_group_destroy(self.h)
+            self.h = None
+
+
+def batch_solve(lib, params_list, images_xfastest, dims_list, max_concurrent, merged=False):
+    """ns3d_batch_solve / ns3d_batch_solve_merged over host images.
+    Returns (results, statuses, group stats or None, return code)."""
+    lib = _declare_server(lib)
+    n = len(params_list)
+    raws = [np.ascontiguousarray(r, dtype=np.uint8).reshape(-1) for r in images_xfastest]
+    ptrs = (_P(C.c_uint8) * n)(*[_ptr(r, C.c_uint8) for r in raws])
+    dims = np.ascontiguousarray(np.array(dims_list, np.int32).reshape(-1))
+    ps = (Params * n)(*params_list)
+    res = (Result * n)()
+    st = np.zeros(n, np.int32)
+    if merged:
+        g = GroupStats()
+        rc = lib.ns3d_batch_solve_merged(ps, ptrs, _ptr(dims, C.c_int32), n, int(max_concurrent), res,
+                                         _ptr(st, C.c_int32), C.byref(g))
+    else:
+        g = None
+        rc = lib.ns3d_batch_solve(ps, ptrs, _ptr(dims, C.c_int32), n, int(max_concurrent), res, _ptr(st, C.c_int32))
+    return list(res), st, g, rc

@@ -122,12 +122,20 @@ struct KSys {  // one system of a solve set (device array)
 constexpr int PART_PER_CHUNK = 20;
 
 // A solve set as a kernel argument (passed by value, read from constant
-// memory): the systems in chunk order, sys[0].chunk_begin == 0.
+// memory): the systems in chunk order, sys[0].chunk_begin == 0.  A solver
+// instance's own sets hold up to KMAX systems (its three momentum
+// components, or its pressure system); a merged set holds the systems of
+// many concurrent solves (up to KMAX_MERGED, 8.7 KB of kernel parameters).
 constexpr int KMAX = 4;
-struct KSetArg {
+constexpr int KMAX_MERGED = 64;
+template <int CAP>
+struct KSetArgT {
     int nsys, total_chunks;
-    KSys sys[KMAX];
+    KSys sys[CAP];
 };
+using KSetArg = KSetArgT<KMAX>;
+using KSetArgMerged = KSetArgT<KMAX_MERGED>;
+static_assert(sizeof(KSetArgMerged) <= 32000, "kernel parameter space");
 
 // The persistent BiCGSTAB loop kernel: block shape and its grid barrier.
 #ifndef NS3D_LOOP_THREADS
@@ -137,7 +145,7 @@ constexpr int LOOP_THREADS = NS3D_LOOP_THREADS;
 constexpr int LOOP_GROUPS = LOOP_THREADS / LANES;
 // blocks per SM the loop kernels are compiled for (64 registers a thread)
 constexpr int LOOP_MIN_BLOCKS = LOOP_THREADS >= 1024 ? 1 : 1024 / LOOP_THREADS;
-static_assert(LOOP_GROUPS >= KMAX, "group s combines the partials of system s");
+static_assert(LOOP_GROUPS >= KMAX, "the FP32 loop kernel: group s combines the partials of system s");
 struct GridBar {  // arrival counter and error flag on separate 128-byte lines
     unsigned int count, pad0_[31];
     int err, pad1_[31];

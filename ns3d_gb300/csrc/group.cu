@@ -1,0 +1,198 @@
+// group.cu -- merged solve sets: the BiCGSTAB work of many concurrent solves
+// in one set of persistent kernels (SolveGroup, runtime.h), and its C-ABI.
+//
+// A member thread queues its set and waits; the first waiting member whose
+// set is still queued becomes the leader: it waits until every member that
+// is solving has queued a set (or window_s passes), takes the queued sets in
+// arrival order up to KMAX_MERGED systems, orders the group stream after
+// each member's stream (an event per set), runs the merged set, copies each
+// system's final state back to its member, and orders each member's stream
+// after the merged launch (a second event per set).  Leaders take turns, one
+// at a time, so the group stream and its set have a single user.
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+
+#include "runtime.h"
+
+namespace ns3d {
+
+struct SolveGroup::Req {
+    const std::vector<SolveItem> *items = nullptr;
+    cudaStream_t st = nullptr;
+    KState *dst = nullptr;
+    std::vector<SolveOutcome> *out = nullptr;
+    cudaEvent_t ready = nullptr, fin = nullptr;
+    bool taken = false, done = false;
+    int err_code = NS3D_OK;
+    std::string err;
+};
+
+SolveGroup::SolveGroup() : set_(new KrylovSetMerged()) {
+    NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+}
+
+SolveGroup::~SolveGroup() {
+    set_.reset();  // its buffers are freed on the group stream
+    if (stream_) {
+        cudaStreamSynchronize(stream_);
+        cudaStreamDestroy(stream_);
+    }
+}
+
+void SolveGroup::join() {
+    std::lock_guard<std::mutex> lk(mu_);
+    members_++;
+}
+
+void SolveGroup::leave() {
+    std::lock_guard<std::mutex> lk(mu_);
+    members_--;
+    cv_.notify_all();  // a leader waiting for this member stops waiting
+}
+
+SolveGroup::Stats SolveGroup::stats() {
+    std::lock_guard<std::mutex> lk(mu_);
+    return stats_;
+}
+
+void SolveGroup::execute(std::vector<Req *> &batch) {
+    auto fail = [&](int code, const std::string &m) {
+        // the members' buffers may still be in use by queued work: drain the
+        // group stream before any member returns with the error
+        cudaStreamSynchronize(stream_);
+        for (Req *q : batch) {
+            q->err_code = code;
+            q->err = m;
+        }
+    };
+    try {
+        std::vector<SolveItem> all;
+        for (Req *q : batch) {
+            NS3D_CUDA_CHECK(cudaStreamWaitEvent(stream_, q->ready, 0));
+            all.insert(all.end(), q->items->begin(), q->items->end());
+        }
+        std::vector<SolveOutcome> out;
+        set_->run(all, stream_, out);
+        size_t off = 0;
+        for (Req *q : batch) {
+            const size_t n = q->items->size();
+            q->out->assign(out.begin() + off, out.begin() + off + n);
+            if (q->dst && n)
+                NS3D_CUDA_CHECK(cudaMemcpyAsync(q->dst, set_->device_state((int)off), n * sizeof(KState),
+                                                cudaMemcpyDeviceToDevice, stream_));
+            NS3D_CUDA_CHECK(cudaEventRecord(q->fin, stream_));
+            off += n;
+        }
+    } catch (const ApiError &e) {
+        fail(e.code, e.what());
+    } catch (const std::bad_alloc &) {
+        fail(NS3D_ERR_OOM, "host allocation failed");
+    } catch (const std::exception &e) {
+        fail(NS3D_ERR_CUDA, e.what());
+    }
+}
+
+void SolveGroup::run(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
+                     std::vector<SolveOutcome> &out) {
+    if ((int)items.size() > KMAX_MERGED) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
+    Req r;
+    r.items = &items;
+    r.st = st;
+    r.dst = state_dst;
+    r.out = &out;
+    struct Events {  // destroyed on every path (a wait already issued keeps its event alive)
+        Req &q;
+        ~Events() {
+            if (q.ready) cudaEventDestroy(q.ready);
+            if (q.fin) cudaEventDestroy(q.fin);
+        }
+    } events{r};
+    NS3D_CUDA_CHECK(cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming));
+    NS3D_CUDA_CHECK(cudaEventCreateWithFlags(&r.fin, cudaEventDisableTiming));
+    NS3D_CUDA_CHECK(cudaEventRecord(r.ready, st));
+    std::unique_lock<std::mutex> lk(mu_);
+    pending_.push_back(&r);
+    cv_.notify_all();
+    while (!r.done) {
+        if (leading_ || r.taken) {
+            cv_.wait(lk);
+            continue;
+        }
+        // lead one merged launch
+        leading_ = true;
+        const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(window_s);
+        cv_.wait_until(lk, deadline, [&] { return (int)pending_.size() >= members_; });
+        std::vector<Req *> batch;
+        batch.reserve(pending_.size());
+        int systems = 0;
+        while (!pending_.empty()) {
+            Req *q = pending_.front();
+            const int n = (int)q->items->size();
+            if (!batch.empty() && systems + n > KMAX_MERGED) break;
+            pending_.pop_front();
+            q->taken = true;
+            batch.push_back(q);
+            systems += n;
+        }
+        stats_.launches++;
+        stats_.requests += (int64_t)batch.size();
+        stats_.systems += systems;
+        stats_.max_systems = std::max(stats_.max_systems, systems);
+        stats_.max_requests = std::max(stats_.max_requests, (int)batch.size());
+        lk.unlock();
+        execute(batch);
+        lk.lock();
+        for (Req *q : batch) q->done = true;
+        leading_ = false;
+        cv_.notify_all();
+    }
+    lk.unlock();
+    if (r.err_code != NS3D_OK) throw ApiError(r.err_code, "merged solve set: " + r.err);
+    NS3D_CUDA_CHECK(cudaStreamWaitEvent(st, r.fin, 0));
+}
+
+}  // namespace ns3d
+
+using namespace ns3d;
+
+struct ns3d_group {
+    SolveGroup g;
+};
+
+extern "C" {
+
+NS3D_API int ns3d_group_create(ns3d_group **out) {
+    if (!out) return report_error(NS3D_ERR_ARG, "NULL argument");
+    try {
+        *out = new ns3d_group();
+        return NS3D_OK;
+    } catch (const CudaError &e) {
+        return report_error(NS3D_ERR_CUDA, e.what());
+    } catch (const std::exception &e) {
+        return report_error(NS3D_ERR_OOM, e.what());
+    }
+}
+
+NS3D_API int ns3d_group_get_stats(ns3d_group *g, ns3d_group_stats *out) {
+    if (!g || !out) return report_error(NS3D_ERR_ARG, "NULL argument");
+    const SolveGroup::Stats s = g->g.stats();
+    std::memset(out, 0, sizeof *out);
+    out->launches = s.launches;
+    out->requests = s.requests;
+    out->systems = s.systems;
+    out->max_systems = s.max_systems;
+    out->max_requests = s.max_requests;
+    return NS3D_OK;
+}
+
+NS3D_API int ns3d_group_destroy(ns3d_group *g) {
+    delete g;
+    return NS3D_OK;
+}
+
+}  // extern "C"
+
+namespace ns3d {
+SolveGroup *group_of(ns3d_group *g) { return g ? &g->g : nullptr; }
+}  // namespace ns3d

@@ -10,7 +10,8 @@ namespace ns3d {
 struct Grid;
 struct SysView;
 struct KSys;
-struct KSetArg;
+template <int CAP>
+struct KSetArgT;
 struct GridBar;
 struct LoopProf;
 struct KState;
@@ -79,11 +80,16 @@ void launch_scatter_image(const int *map, long ncells, const double *img, double
 void launch_face_average(const Grid &g, const double *u, const double *v, const double *w, double *vavg,
                          cudaStream_t st);
 
-// krylov.cu: batched BiCGSTAB over a set of systems
-void launch_krylov_init(const KSetArg &set, cudaStream_t st);
+// krylov.cu: batched BiCGSTAB over a set of systems (instantiated for the
+// set capacities KMAX and KMAX_MERGED)
+template <int CAP>
+void launch_krylov_init(const KSetArgT<CAP> &set, cudaStream_t st);
 // iterations until every system is done, one needs a restart, or max_iters
-cudaError_t launch_krylov_loop(const KSetArg &set, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st);
-void launch_krylov_restart(const KSetArg &set, cudaStream_t st);
+template <int CAP>
+cudaError_t launch_krylov_loop(const KSetArgT<CAP> &set, GridBar *bar, LoopProf *prof, int max_iters,
+                               cudaStream_t st);
+template <int CAP>
+void launch_krylov_restart(const KSetArgT<CAP> &set, cudaStream_t st);
 // blocks of a loop-kernel launch over `units` work units, units_per_chunk
 // of them per 1024-row chunk (occ blocks per SM)
 int loop_grid(int units, int units_per_chunk, int occ);

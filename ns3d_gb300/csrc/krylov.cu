@@ -100,13 +100,26 @@ __device__ __forceinline__ Row4 spmv4(const KSys &S, int r0, const double *__res
     return out;
 }
 
-// system owning global chunk c (chunk_begin ascending, first system begins at 0)
-__device__ __forceinline__ int sys_of_chunk(const KSetArg &A, int c) {
-    int s = 0;
+// system owning global chunk c (chunk_begin ascending, first system begins
+// at 0; a system without rows shares its chunk_begin with the next one, and
+// both forms pick the last system whose first chunk is <= c)
+template <int CAP>
+__device__ __forceinline__ int sys_of_chunk(const KSetArgT<CAP> &A, int c) {
+    if constexpr (CAP <= KMAX) {
+        int s = 0;
 #pragma unroll
-    for (int q = 1; q < KMAX; ++q)
-        if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
-    return s;
+        for (int q = 1; q < CAP; ++q)
+            if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
+        return s;
+    } else {
+        int lo = 0, hi = A.nsys - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (c >= A.sys[mid].chunk_begin) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
 }
 
 // the done/paused flags change only between kernels (or after the last
@@ -143,7 +156,8 @@ __device__ __forceinline__ void finish_loop(KState *st) {
         const int r0 = lc * CH + threadIdx.x;
 
 // ---- init: r = b - A x, r0 = r, |r|^2, |b|^2 ---------------------------------
-__global__ void __launch_bounds__(LANES) k_kr_init(const __grid_constant__ KSetArg A) {
+template <int CAP>
+__global__ void __launch_bounds__(LANES) k_kr_init(const __grid_constant__ KSetArgT<CAP> A) {
     __shared__ double sm[LANES];
     __shared__ int sh[2];
     NS3D_CHUNK_LOOP
@@ -210,7 +224,8 @@ __global__ void __launch_bounds__(LANES) k_kr_init(const __grid_constant__ KSetA
 }
 
 // p = v = 0; x = 0 for a zero right-hand side
-__global__ void k_kr_init2(const __grid_constant__ KSetArg A) {
+template <int CAP>
+__global__ void k_kr_init2(const __grid_constant__ KSetArgT<CAP> A) {
     NS3D_CHUNK_LOOP
         Row4 z;
 #pragma unroll
@@ -228,10 +243,11 @@ __global__ void k_kr_init2(const __grid_constant__ KSetArg A) {
 // reduction order) and reduces them with a named barrier.  Every block keeps
 // a copy of the per-system scalars in shared memory; after each grid-wide
 // barrier every block combines the chunk partials of each system in the
-// fixed order itself (group s for system s), so all copies stay bit-identical
-// without a broadcast.  Partials of the three reductions of an iteration go
-// to separate regions of S.part, so a block that runs ahead never overwrites
-// partials another block is still combining:
+// fixed order itself (group g for systems g, g + LOOP_GROUPS, ...), so all
+// copies stay bit-identical without a broadcast.  Partials of the three
+// reductions of an iteration go to separate regions of S.part, so a block
+// that runs ahead never overwrites partials another block is still
+// combining:
 //   [0, 2n)  <t,t>, <t,s> pairs     [2n, 4n)  <r0,r>, <r,r> pairs
 //   [4n, 5n) <r0,v>
 // The loop ends when every system is done, when a system needs a restart
@@ -246,9 +262,11 @@ constexpr int kSpmvUnroll = NS3D_SPMV_UNROLL;
 
 __device__ __forceinline__ bool state_active(const KState &k) { return (k.done | k.paused) == 0; }
 
+template <int CAP>
 __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
-    k_kr_loop(const __grid_constant__ KSetArg A, GridBar *bar, LoopProf *prof, int max_iters) {
-    __shared__ KState sst[KMAX];
+    k_kr_loop(const __grid_constant__ KSetArgT<CAP> A, GridBar *bar, LoopProf *prof, int max_iters) {
+    static_assert(CAP <= LOOP_THREADS, "one thread copies each system's state");
+    __shared__ KState sst[CAP];
     __shared__ double sm[LOOP_GROUPS][LANES];
     __shared__ int s_ok;
     const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
@@ -313,10 +331,11 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
         }
         if (!(ok = grid_sync(bar, target, &s_ok))) break;
-        if (gi < A.nsys && state_active(sst[gi])) {
-            const KSys &S = A.sys[gi];
+        for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+            if (!state_active(sst[q])) continue;
+            const KSys &S = A.sys[q];
             const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks, S.nchunks, 1, lane, sm[gi], gsync);
-            if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+            if (lane == 0) sst[q].alpha = sst[q].rho / d;
         }
         __syncthreads();
         mark(1);
@@ -360,11 +379,12 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
         }
         if (!(ok = grid_sync(bar, target, &s_ok))) break;
-        if (gi < A.nsys && state_active(sst[gi])) {
-            const KSys &S = A.sys[gi];
+        for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+            if (!state_active(sst[q])) continue;
+            const KSys &S = A.sys[q];
             double ftt, fts;
             lanes_final_sum2(S.part, S.nchunks, lane, sm[gi], ftt, fts, gsync);
-            if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+            if (lane == 0) sst[q].w = (ftt > 0.0) ? fts / ftt : 0.0;
         }
         __syncthreads();
         mark(3);
@@ -394,12 +414,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             if (lane == 0) reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks)[lc] = make_double2(t0r, trr);
         }
         if (!(ok = grid_sync(bar, target, &s_ok))) break;
-        if (gi < A.nsys && state_active(sst[gi])) {
-            const KSys &S = A.sys[gi];
+        for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+            if (!state_active(sst[q])) continue;
+            const KSys &S = A.sys[q];
             double f0r, frr;
             lanes_final_sum2(S.part + 2 * (size_t)S.nchunks, S.nchunks, lane, sm[gi], f0r, frr, gsync);
             if (lane == 0) {
-                KState *st = &sst[gi];
+                KState *st = &sst[q];
                 st->rr = frr;
                 st->iter += 1;
                 st->work += 1;
@@ -419,9 +440,18 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
         __syncthreads();
         mark(4);
         bool any_active = false, any_paused = false;
-        for (int q = 0; q < A.nsys; ++q) {
-            any_active = any_active || state_active(sst[q]);
-            any_paused = any_paused || (sst[q].paused != 0 && sst[q].done == 0);
+        if constexpr (CAP <= KMAX) {
+            for (int q = 0; q < A.nsys; ++q) {
+                any_active = any_active || state_active(sst[q]);
+                any_paused = any_paused || (sst[q].paused != 0 && sst[q].done == 0);
+            }
+        } else {  // the lanes of each warp split the systems
+            for (int q = threadIdx.x & 31; q < A.nsys; q += 32) {
+                any_active = any_active || state_active(sst[q]);
+                any_paused = any_paused || (sst[q].paused != 0 && sst[q].done == 0);
+            }
+            any_active = __any_sync(0xffffffffu, any_active);
+            any_paused = __any_sync(0xffffffffu, any_paused);
         }
         if (!any_active || any_paused) {
             ++it;
@@ -441,7 +471,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
 }
 
 // restart of paused systems: r = b - A x, r0 = r, rho = |r0|^2
-__global__ void __launch_bounds__(LANES) k_kr_restart(const __grid_constant__ KSetArg A) {
+template <int CAP>
+__global__ void __launch_bounds__(LANES) k_kr_restart(const __grid_constant__ KSetArgT<CAP> A) {
     __shared__ double sm[LANES];
     __shared__ int sh[2];
     NS3D_CHUNK_LOOP
@@ -508,11 +539,12 @@ int device_sm_count() {
 // waves); beyond that, blocks walk the chunks grid-stride
 static inline int kr_grid(int total_chunks) { return std::max(1, std::min(total_chunks, device_sm_count() * 32)); }
 
-void launch_krylov_init(const KSetArg &A, cudaStream_t st) {
+template <int CAP>
+void launch_krylov_init(const KSetArgT<CAP> &A, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
     count_launches(2);
-    k_kr_init<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
-    k_kr_init2<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_kr_init<CAP><<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_kr_init2<CAP><<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
 // Blocks of a loop-kernel launch.  Every block must be resident at once
@@ -538,31 +570,48 @@ int loop_grid(int units, int units_per_chunk, int occ) {
     return std::max(1, std::min(std::max(dense, std::min(fair, units)), slots));
 }
 
-static std::atomic<int> g_loop_occ{0};
+// A merged set (the systems of many concurrent solves) spreads over every SM.
+template <int CAP>
+static int krylov_loop_grid(int total_chunks, int occ) {
+    if (CAP > KMAX) return std::max(1, std::min(total_chunks, device_sm_count() * std::max(occ, 1)));
+    return loop_grid(total_chunks, 1, occ);
+}
 
-cudaError_t launch_krylov_loop(const KSetArg &A, GridBar *bar, LoopProf *prof, int max_iters, cudaStream_t st) {
+template <int CAP>
+cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *prof, int max_iters,
+                               cudaStream_t st) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
-    int occ = g_loop_occ.load();
+    static std::atomic<int> loop_occ{0};
+    int occ = loop_occ.load();
     if (occ == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kr_loop, LOOP_THREADS, 0);
+        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kr_loop<CAP>, LOOP_THREADS, 0);
         if (e != cudaSuccess) return e;
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
-        g_loop_occ = occ;
+        loop_occ = occ;
     }
-    const int grid = loop_grid(A.total_chunks, 1, occ);
+    const int grid = krylov_loop_grid<CAP>(A.total_chunks, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
-    KSetArg a = A;
+    KSetArgT<CAP> a = A;
     void *args[] = {&a, &bar, &prof, &max_iters};
     count_launches(1);
-    return cudaLaunchCooperativeKernel((const void *)k_kr_loop, grid, LOOP_THREADS, args, 0, st);
+    return cudaLaunchCooperativeKernel((const void *)k_kr_loop<CAP>, grid, LOOP_THREADS, args, 0, st);
 }
 
-void launch_krylov_restart(const KSetArg &A, cudaStream_t st) {
+template <int CAP>
+void launch_krylov_restart(const KSetArgT<CAP> &A, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_kr_restart<<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_kr_restart<CAP><<<kr_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
+
+template void launch_krylov_init<KMAX>(const KSetArg &, cudaStream_t);
+template void launch_krylov_init<KMAX_MERGED>(const KSetArgMerged &, cudaStream_t);
+template cudaError_t launch_krylov_loop<KMAX>(const KSetArg &, GridBar *, LoopProf *, int, cudaStream_t);
+template cudaError_t launch_krylov_loop<KMAX_MERGED>(const KSetArgMerged &, GridBar *, LoopProf *, int,
+                                                     cudaStream_t);
+template void launch_krylov_restart<KMAX>(const KSetArg &, cudaStream_t);
+template void launch_krylov_restart<KMAX_MERGED>(const KSetArgMerged &, cudaStream_t);
 
 void launch_spmv(const SysView &A, const double *x, double *y, cudaStream_t st) {
     if (A.n <= 0) return;

@@ -3,7 +3,10 @@
 
 #include <cuda_runtime.h>
 
+#include <condition_variable>
+#include <deque>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -160,11 +163,18 @@ struct OwnedStream {
     }
 };
 
-// A set of up to KMAX systems solved together by the BiCGSTAB loop kernel.
-class KrylovSet {
+// A set of up to CAP systems solved together by the BiCGSTAB loop kernel
+// (KrylovSet: one solver instance's systems; KrylovSetMerged: the systems of
+// many concurrent solves, see SolveGroup).
+template <int CAP>
+class KrylovSetT {
   public:
     void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out);
     const KState *device_state(int i) const { return st_.p + i; }
+    // allocates the per-system state of `items` (and records them) without
+    // solving: a merged run copies the final states here
+    void prepare(const std::vector<SolveItem> &items, cudaStream_t st) { configure(items, st); }
+    KState *state_buffer() { return st_.p; }
     long launches() const { return launches_; }
     void reset_launch_count() { launches_ = 0; }
 
@@ -178,12 +188,12 @@ class KrylovSet {
     };
     bool profiling = false;
     Profile prof;
-    ~KrylovSet();
+    ~KrylovSetT();
 
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
     cudaEvent_t ev_[2] = {nullptr, nullptr};
-    KSetArg set_;  // passed to every kernel by value
+    KSetArgT<CAP> set_;  // passed to every kernel by value
     DBuf<KState> st_;
     HBuf<KState> h_st_, h_up_;
     DBuf<GridBar> bar_;
@@ -192,6 +202,53 @@ class KrylovSet {
     int nsys_ = 0, total_chunks_ = 0;
     long launches_ = 0;
 };
+using KrylovSet = KrylovSetT<KMAX>;
+using KrylovSetMerged = KrylovSetT<KMAX_MERGED>;
+
+// The FP64 solves of many concurrent solver instances merged into one set of
+// persistent kernels: each member's BiCGSTAB sets (its momentum components,
+// its pressure system) are queued here, and one member at a time (the
+// leader) gathers every queued set, up to KMAX_MERGED systems, and solves
+// them with one loop launch per round over the ragged list of their
+// 1024-row chunks, on the group's own stream.  The leader waits for the
+// other members up to a short window (the members run their outer
+// iterations in near lockstep), so the launches stay full.  Each system
+// keeps its own scalars and reduction order, so a solve gives the same bits
+// alone and merged.
+class SolveGroup {
+  public:
+    SolveGroup();
+    ~SolveGroup();
+    // a solve of a member starts / ends (the leader waits for members only)
+    void join();
+    void leave();
+    // Solves `items` (whose inputs are ready on `st`) with whatever else the
+    // members queue meanwhile.  On return `out` holds the outcomes, the
+    // final state of item i is in state_dst[i] (device), and work queued on
+    // `st` afterwards runs after the merged launch.
+    void run(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
+             std::vector<SolveOutcome> &out);
+    struct Stats {
+        int64_t launches = 0, requests = 0, systems = 0;
+        int max_systems = 0, max_requests = 0;
+    };
+    Stats stats();
+    double window_s = 2e-3;  // longest wait of a leader for the other members
+
+  private:
+    struct Req;
+    void execute(std::vector<Req *> &batch);
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<Req *> pending_;
+    int members_ = 0;
+    bool leading_ = false;
+    Stats stats_;
+    cudaStream_t stream_ = nullptr;
+    std::unique_ptr<KrylovSetMerged> set_;
+};
+// the solve group behind a C-ABI group handle (NULL for NULL)
+SolveGroup *group_of(ns3d_group *g);
 
 struct DCState;
 

@@ -61,11 +61,12 @@ struct Job {
     Clock::time_point submitted, started, finished;
 };
 
-int run_one(Job &j) {
+int run_one(Job &j, ns3d_group *group) {
     ns3d_handle *h = nullptr;
     int rc = ns3d_open(&j.params, j.raw.data(), j.nx, j.ny, j.nz, &h);
     if (rc != NS3D_OK) return rc;
-    rc = ns3d_solve(h);
+    if (group) rc = ns3d_set_group(h, group);
+    if (rc == NS3D_OK) rc = ns3d_solve(h);
     if (rc == NS3D_OK) rc = ns3d_get_result(h, &j.result);
     if (rc == NS3D_OK && j.keep_fields) {
         ns3d_sizes s;
@@ -99,6 +100,7 @@ struct ns3d_server {
     Clock::time_point first_submit, last_finish;
     bool any = false;
     int64_t completed = 0, failed = 0;
+    ns3d_group *group = nullptr;  // merged solve sets (ns3d_server_set_merging)
 
     // device memory available to a new solve: free memory plus what the
     // library pool holds released by finished solves (queried without the
@@ -151,7 +153,7 @@ struct ns3d_server {
 
     void work(Job *j) {
         cudaSetDevice(device);
-        int rc = run_one(*j);
+        int rc = run_one(*j, group);
         if (rc != NS3D_OK) {
             j->error = ns3d_last_error();  // the worker thread's error text
             std::fprintf(stderr, "ns3d server: request %lld failed (%d): %s\n", (long long)j->ticket, rc,
@@ -305,16 +307,43 @@ NS3D_API int ns3d_server_stop(ns3d_server *s) {
         std::unique_lock<std::mutex> lk(s->mu);
         s->done_cv.wait(lk, [&] { return s->active == 0; });
     }
+    if (s->group) ns3d_group_destroy(s->group);
     delete s;
     return NS3D_OK;
 }
 
-NS3D_API int ns3d_batch_solve(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
-                              int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status) {
+NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t enable) {
+    if (!s) return NS3D_ERR_ARG;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->any) return NS3D_ERR_STATE;  // before the first request only
+    if (enable && !s->group) {
+        cudaSetDevice(s->device);
+        const int rc = ns3d_group_create(&s->group);
+        if (rc != NS3D_OK) return rc;
+    } else if (!enable && s->group) {
+        ns3d_group_destroy(s->group);
+        s->group = nullptr;
+    }
+    return NS3D_OK;
+}
+
+NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out) {
+    if (!s || !out) return NS3D_ERR_ARG;
+    std::memset(out, 0, sizeof *out);
+    return s->group ? ns3d_group_get_stats(s->group, out) : NS3D_OK;
+}
+
+static int batch_solve(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims, int32_t njobs,
+                       int32_t max_concurrent, int32_t merge, ns3d_result *results, int32_t *status,
+                       ns3d_group_stats *gstats) {
     if (!params || !raws || !dims || !results || njobs < 0 || max_concurrent <= 0) return NS3D_ERR_ARG;
     ns3d_server *s = nullptr;
     int rc = ns3d_server_start(max_concurrent, 0, &s);
     if (rc != NS3D_OK) return rc;
+    if (merge && (rc = ns3d_server_set_merging(s, 1)) != NS3D_OK) {
+        ns3d_server_stop(s);
+        return rc;
+    }
     std::vector<int64_t> tickets((size_t)njobs);
     for (int i = 0; i < njobs; ++i) {
         rc = ns3d_server_submit(s, &params[i], raws[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], 0,
@@ -330,8 +359,20 @@ NS3D_API int ns3d_batch_solve(const ns3d_params *params, const uint8_t *const *r
         if (status) status[i] = r;
         if (r != NS3D_OK) worst = r;
     }
+    if (gstats) ns3d_server_group_stats(s, gstats);
     ns3d_server_stop(s);
     return worst;
+}
+
+NS3D_API int ns3d_batch_solve(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                              int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status) {
+    return batch_solve(params, raws, dims, njobs, max_concurrent, 0, results, status, nullptr);
+}
+
+NS3D_API int ns3d_batch_solve_merged(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                                     int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status,
+                                     ns3d_group_stats *stats) {
+    return batch_solve(params, raws, dims, njobs, max_concurrent, 1, results, status, stats);
 }
 
 }  // extern "C"

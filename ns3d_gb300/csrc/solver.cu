@@ -78,7 +78,8 @@ size_t pool_cached_bytes() {
     return reserved > used ? (size_t)(reserved - used) : 0;
 }
 
-void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
+template <int CAP>
+void KrylovSetT<CAP>::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     std::vector<KSys> ks;
     int chunk = 0;
     for (const SolveItem &it : items) {
@@ -101,7 +102,7 @@ void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) 
         ks.push_back(k);
     }
     const int ns = (int)ks.size();
-    if (ns > KMAX) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
+    if (ns > CAP) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     if ((int)st_.n < ns) {
         st_.alloc_zero(ns, st);
         h_st_.alloc(ns);
@@ -124,7 +125,9 @@ void KrylovSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) 
     total_chunks_ = chunk;
 }
 
-void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out) {
+template <int CAP>
+void KrylovSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st,
+                          std::vector<SolveOutcome> &out) {
     configure(items, st);
     const int ns = nsys_;
     out.assign(ns, SolveOutcome());
@@ -214,10 +217,14 @@ void KrylovSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::v
     }
 }
 
-KrylovSet::~KrylovSet() {
+template <int CAP>
+KrylovSetT<CAP>::~KrylovSetT() {
     for (cudaEvent_t e : ev_)
         if (e) cudaEventDestroy(e);
 }
+
+template class KrylovSetT<KMAX>;
+template class KrylovSetT<KMAX_MERGED>;
 
 // ============================ solver instance ================================
 static thread_local std::string g_err;
@@ -255,10 +262,20 @@ struct ns3d_handle {
     HBuf<DiagOut> h_diag;
     KrylovSet kmom, kp;
     MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
+    SolveGroup *group = nullptr;  // FP64 sets merged with other solves' (ns3d_set_group)
     bool mixed() const { return prm.precision != NS3D_FP64; }
+    // an FP64 set: alone, or merged with the sets of the group's other solves
+    void run_fp64(KrylovSet &own, const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
+        if (!group) {
+            own.run(items, stream, out);
+            return;
+        }
+        own.prepare(items, stream);  // the merged run leaves the final states here
+        group->run(items, stream, own.state_buffer(), out);
+    }
     void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
         if (mixed()) mp.run(items, stream, out);
-        else kp.run(items, stream, out);
+        else run_fp64(kp, items, out);
     }
 
     // physical constants and relaxation state (NavierStokesBase members)
@@ -440,7 +457,7 @@ void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
     if (nw > 0) items.push_back({&W, w.p, W.rhs.p, prm.vsolvertol, prm.maxitsolver});
     std::vector<SolveOutcome> out;
     if (mixed()) mmom.run(items, stream, out);
-    else kmom.run(items, stream, out);
+    else run_fp64(kmom, items, out);
     auto state = [&](int i) { return mixed() ? mmom.device_state(i) : kmom.device_state(i); };
     launch_velocity_post(utemp.p, u.p, nu, state(0), limit, dvmax, stream);
     launch_velocity_post(vtemp.p, v.p, nv, state(1), limit, dvmax, stream);
@@ -1050,6 +1067,15 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
     h.kp.reset_launch_count();
     // while several solves run at once the loop kernels take fewer SMs each
     ActiveSolve active;
+    struct Member {  // a merged solve counts as a member of its group while it runs
+        SolveGroup *g;
+        explicit Member(SolveGroup *grp) : g(grp) {
+            if (g) g->join();
+        }
+        ~Member() {
+            if (g) g->leave();
+        }
+    } member(h.mixed() ? nullptr : h.group);
     if (h.prm.method == NS3D_SIMPLEC) h.run_simplec();
     else h.run_simpler_family(h.prm.method);
     return NS3D_OK;
@@ -1079,6 +1105,13 @@ NS3D_API int ns3d_solve_sweep(ns3d_handle *H, const double *gradp, int32_t n, in
         if (rc != NS3D_OK) return rc;
         results[i] = h.res;
     }
+    return NS3D_OK;
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_set_group(ns3d_handle *H, ns3d_group *g) {
+    NS3D_TRY
+    checked(H)->group = group_of(g);
     return NS3D_OK;
     NS3D_CATCH
 }

@@ -44,7 +44,9 @@ def test_oracle_exports_the_solver_symbols(oracle):
                  "ns3d_set_profiling", "ns3d_get_profile", "ns3d_batch_solve", "ns3d_server_start",
                  "ns3d_server_submit", "ns3d_server_poll", "ns3d_server_wait", "ns3d_server_fields",
                  "ns3d_server_get_stats", "ns3d_server_stop", "ns3d_generate_image",
-                 "ns3d_server_cancel_queued", "ns3d_solve_sweep"}
+                 "ns3d_server_cancel_queued", "ns3d_solve_sweep", "ns3d_group_create", "ns3d_set_group",
+                 "ns3d_group_get_stats", "ns3d_group_destroy", "ns3d_server_set_merging",
+                 "ns3d_server_group_stats", "ns3d_batch_solve_merged"}
     for s in declared_symbols():
         if s not in host_only:
             assert hasattr(oracle, s), s
