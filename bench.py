@@ -362,12 +362,13 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
                             "K_rel_err_vs_fp64": rel}}
 
 
-# Merged sample (opt-in, --merged): the batch mix above in plain FP64 (SIMPLEC,
-# flow x), solved one image at a time, as a batch of concurrent solves on
-# their own streams (ns3d_batch_solve), and as a batch whose BiCGSTAB sets are
-# merged into shared persistent launches (ns3d_batch_solve_merged).  The three
-# legs follow the same trajectory bit for bit (fixed-order reductions), so
-# max_outer may cap the outer iterations of every leg alike.
+# Merged sample (opt-in, --merged): the batch mix above (SIMPLEC, flow x)
+# solved in plain FP64 one image at a time, then as batches of concurrent
+# solves on their own streams (ns3d_batch_solve) and with their BiCGSTAB sets
+# merged into shared persistent launches (ns3d_batch_solve_merged), in plain
+# FP64 and in the serving precision.  The FP64 legs follow the same
+# trajectory bit for bit (fixed-order reductions), so max_outer may cap the
+# outer iterations of every leg alike.
 MERGED_IMAGES = 16
 
 
@@ -384,8 +385,8 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
         imgs.append({"shape": shape, "raw": np.ascontiguousarray(img.transpose(2, 1, 0)).reshape(-1),
                      "kind": kind, "phi": ach, "direction": 1, "method": 0})
 
-    def prm(r):
-        p = request_params(capi, lib, r, 0)
+    def prm(r, precision=0):
+        p = request_params(capi, lib, r, precision)
         p.maxitSIMPLE = max_outer
         return p
 
@@ -402,16 +403,22 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
     legs = {"plain_fp64_one_at_a_time": {"solves_per_s": n_images / t1, "seconds": t1,
                                          "cell_updates_per_s": cells / t1,
                                          "bicgstab_row_iterations_per_s": rows / t1}}
-    for name, merged in (("batch_fp64_streams", False), ("batch_fp64_merged", True)):
+    mixed = "mixed_mg" if SERVE_PRECISION == 2 else "mixed"
+    for name, merged, precision in (("batch_fp64_streams", False, 0), ("batch_fp64_merged", True, 0),
+                                    ("batch_%s_streams" % mixed, False, SERVE_PRECISION),
+                                    ("batch_%s_merged" % mixed, True, SERVE_PRECISION)):
         t = time.perf_counter()
-        res, status, g, rc = capi.batch_solve(lib, [prm(r) for r in imgs], [r["raw"] for r in imgs],
+        res, status, g, rc = capi.batch_solve(lib, [prm(r, precision) for r in imgs], [r["raw"] for r in imgs],
                                               [r["shape"] for r in imgs], max_concurrent, merged=merged)
         dt = time.perf_counter() - t
         leg = {"solves_per_s": n_images / dt, "seconds": dt, "status": int(rc),
-               "speedup_vs_one_at_a_time": t1 / dt, "cell_updates_per_s": cells / dt,
-               "bicgstab_row_iterations_per_s": rows / dt,
-               "K_bit_identical_to_one_at_a_time": all(x.K == k for x, k in zip(res, k1)),
-               "max_concurrent": max_concurrent}
+               "speedup_vs_one_at_a_time": t1 / dt, "max_concurrent": max_concurrent}
+        if precision == 0:
+            leg.update({"cell_updates_per_s": cells / dt, "bicgstab_row_iterations_per_s": rows / dt,
+                        "K_bit_identical_to_one_at_a_time": all(x.K == k for x, k in zip(res, k1))})
+        else:
+            leg["max_K_rel_err_vs_fp64"] = max(abs(x.K - k) / abs(k) for x, k in zip(res, k1))
+            leg["outer_iterations"] = [int(x.iterations) for x in res]
         if g is not None:
             leg["group"] = g.as_dict()
             leg["mean_systems_per_set"] = g.systems / max(g.launches, 1)

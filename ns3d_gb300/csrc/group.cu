@@ -3,12 +3,14 @@
 //
 // A member thread queues its set and waits; the first waiting member whose
 // set is still queued becomes the leader: it waits until every member that
-// is solving has queued a set (or window_s passes), takes the queued sets in
-// arrival order up to KMAX_MERGED systems, orders the group stream after
-// each member's stream (an event per set), runs the merged set, copies each
-// system's final state back to its member, and orders each member's stream
-// after the merged launch (a second event per set).  Leaders take turns, one
-// at a time, so the group stream and its set have a single user.
+// is solving has queued a set (or window_s passes), takes the oldest queued
+// set and the later ones of the same kind in arrival order, up to the
+// merged capacity (KMAX_MERGED FP64 or KMAX_MERGED_M mixed systems), orders
+// the group stream after each member's stream (an event per set), runs the
+// merged set, copies each system's final state back to its member, and
+// orders each member's stream after the merged launch (a second event per
+// set).  Leaders take turns, one at a time, so the group stream and its sets
+// have a single user.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -18,6 +20,7 @@
 namespace ns3d {
 
 struct SolveGroup::Req {
+    int kind = 0;  // 0: FP64; 1 + v: mixed precision, FP32 loop variant v
     const std::vector<SolveItem> *items = nullptr;
     cudaStream_t st = nullptr;
     KState *dst = nullptr;
@@ -28,12 +31,13 @@ struct SolveGroup::Req {
     std::string err;
 };
 
-SolveGroup::SolveGroup() : set_(new KrylovSetMerged()) {
+SolveGroup::SolveGroup() : set_(new KrylovSetMerged()), mset_(new MixedSetMerged()) {
     NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
 }
 
 SolveGroup::~SolveGroup() {
-    set_.reset();  // its buffers are freed on the group stream
+    set_.reset();  // their buffers are freed on the group stream
+    mset_.reset();
     if (stream_) {
         cudaStreamSynchronize(stream_);
         cudaStreamDestroy(stream_);
@@ -73,14 +77,17 @@ void SolveGroup::execute(std::vector<Req *> &batch) {
             all.insert(all.end(), q->items->begin(), q->items->end());
         }
         std::vector<SolveOutcome> out;
-        set_->run(all, stream_, out);
+        const int kind = batch.front()->kind;
+        if (kind == 0) set_->run(all, stream_, out);
+        else mset_->run(all, stream_, out, kind - 1);
         size_t off = 0;
         for (Req *q : batch) {
             const size_t n = q->items->size();
             q->out->assign(out.begin() + off, out.begin() + off + n);
+            const KState *src = kind == 0 ? set_->device_state((int)off) : mset_->device_state((int)off);
             if (q->dst && n)
-                NS3D_CUDA_CHECK(cudaMemcpyAsync(q->dst, set_->device_state((int)off), n * sizeof(KState),
-                                                cudaMemcpyDeviceToDevice, stream_));
+                NS3D_CUDA_CHECK(
+                    cudaMemcpyAsync(q->dst, src, n * sizeof(KState), cudaMemcpyDeviceToDevice, stream_));
             NS3D_CUDA_CHECK(cudaEventRecord(q->fin, stream_));
             off += n;
         }
@@ -95,12 +102,30 @@ void SolveGroup::execute(std::vector<Req *> &batch) {
 
 void SolveGroup::run(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
                      std::vector<SolveOutcome> &out) {
-    if ((int)items.size() > KMAX_MERGED) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     Req r;
     r.items = &items;
     r.st = st;
     r.dst = state_dst;
     r.out = &out;
+    submit(r);
+}
+
+void SolveGroup::run_mixed(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
+                           std::vector<SolveOutcome> &out, int variant) {
+    Req r;
+    r.kind = 1 + (variant == 1 ? 1 : 0);
+    r.items = &items;
+    r.st = st;
+    r.dst = state_dst;
+    r.out = &out;
+    submit(r);
+}
+
+static int capacity(int kind) { return kind == 0 ? KMAX_MERGED : KMAX_MERGED_M; }
+
+void SolveGroup::submit(Req &r) {
+    if ((int)r.items->size() > capacity(r.kind))
+        throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     struct Events {  // destroyed on every path (a wait already issued keeps its event alive)
         Req &q;
         ~Events() {
@@ -110,7 +135,7 @@ void SolveGroup::run(const std::vector<SolveItem> &items, cudaStream_t st, KStat
     } events{r};
     NS3D_CUDA_CHECK(cudaEventCreateWithFlags(&r.ready, cudaEventDisableTiming));
     NS3D_CUDA_CHECK(cudaEventCreateWithFlags(&r.fin, cudaEventDisableTiming));
-    NS3D_CUDA_CHECK(cudaEventRecord(r.ready, st));
+    NS3D_CUDA_CHECK(cudaEventRecord(r.ready, r.st));
     std::unique_lock<std::mutex> lk(mu_);
     pending_.push_back(&r);
     cv_.notify_all();
@@ -123,14 +148,21 @@ void SolveGroup::run(const std::vector<SolveItem> &items, cudaStream_t st, KStat
         leading_ = true;
         const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(window_s);
         cv_.wait_until(lk, deadline, [&] { return (int)pending_.size() >= members_; });
+        // the oldest queued set and the later ones of its kind, in arrival
+        // order, while they fit
         std::vector<Req *> batch;
         batch.reserve(pending_.size());
         int systems = 0;
-        while (!pending_.empty()) {
-            Req *q = pending_.front();
+        const int kind = pending_.front()->kind;
+        for (auto it = pending_.begin(); it != pending_.end();) {
+            Req *q = *it;
             const int n = (int)q->items->size();
-            if (!batch.empty() && systems + n > KMAX_MERGED) break;
-            pending_.pop_front();
+            if (q->kind != kind) {
+                ++it;
+                continue;
+            }
+            if (!batch.empty() && systems + n > capacity(kind)) break;
+            it = pending_.erase(it);
             q->taken = true;
             batch.push_back(q);
             systems += n;
@@ -149,7 +181,7 @@ void SolveGroup::run(const std::vector<SolveItem> &items, cudaStream_t st, KStat
     }
     lk.unlock();
     if (r.err_code != NS3D_OK) throw ApiError(r.err_code, "merged solve set: " + r.err);
-    NS3D_CUDA_CHECK(cudaStreamWaitEvent(st, r.fin, 0));
+    NS3D_CUDA_CHECK(cudaStreamWaitEvent(r.st, r.fin, 0));
 }
 
 }  // namespace ns3d

@@ -86,13 +86,26 @@ __device__ __forceinline__ double spmv_f64_row(const MSys &S, int row, const dou
                        [&](double acc, int s, int col) { return __fma_rn(cf[(size_t)s * np], x[col], acc); });
 }
 
-// system owning global chunk c (systems in chunk order, first begins at 0)
-__device__ __forceinline__ int msys_of_chunk(const MSetArg &A, int c) {
-    int s = 0;
+// system owning global chunk c (systems in chunk order, first begins at 0;
+// the last system whose first chunk is <= c, so a system without rows is
+// never chosen)
+template <int CAP>
+__device__ __forceinline__ int msys_of_chunk(const MSetArgT<CAP> &A, int c) {
+    if constexpr (CAP <= KMAX) {
+        int s = 0;
 #pragma unroll
-    for (int q = 1; q < KMAX; ++q)
-        if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
-    return s;
+        for (int q = 1; q < CAP; ++q)
+            if (q < A.nsys && c >= A.sys[q].chunk_begin) s = q;
+        return s;
+    } else {
+        int lo = 0, hi = A.nsys - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (c >= A.sys[mid].chunk_begin) lo = mid;
+            else hi = mid - 1;
+        }
+        return lo;
+    }
 }
 
 // Flags change only between kernels (or in the last block of a system, after
@@ -127,7 +140,8 @@ __device__ __forceinline__ bool m_arrive_last(unsigned int *counter, unsigned in
 __device__ __forceinline__ bool finite(double x) { return isfinite(x); }
 
 // ---- FP64 residual and outer control -----------------------------------------
-__global__ void __launch_bounds__(LANES) k_dc_resid(const __grid_constant__ MSetArg A, int first) {
+template <int CAP>
+__global__ void __launch_bounds__(LANES) k_dc_resid(const __grid_constant__ MSetArgT<CAP> A, int first) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
     NS3D_MCHUNK_LOOP(false)
@@ -193,7 +207,8 @@ __global__ void __launch_bounds__(LANES) k_dc_resid(const __grid_constant__ MSet
 }
 
 // x64 = 0 for systems with a zero right-hand side (first round)
-__global__ void k_dc_zero(const __grid_constant__ MSetArg A) {
+template <int CAP>
+__global__ void k_dc_zero(const __grid_constant__ MSetArgT<CAP> A) {
     for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
         const MSys &S = A.sys[msys_of_chunk(A, c)];
         if (!__ldcg(&S.dc->zero_rhs)) continue;
@@ -204,7 +219,8 @@ __global__ void k_dc_zero(const __grid_constant__ MSetArg A) {
 }
 
 // ---- FP32 inner solve -------------------------------------------------------
-__global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSetArg A) {
+template <int CAP>
+__global__ void __launch_bounds__(LANES) k_m32_init(const __grid_constant__ MSetArgT<CAP> A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
     NS3D_MCHUNK_LOOP(true)
@@ -354,6 +370,124 @@ __device__ bool mg_apply(const MSys &S, const float *b0, float *x0, GridBar *bar
     return true;
 }
 
+// the inner solve of a system runs (its outer solve is not done either)
+__device__ __forceinline__ bool inner_active(const KState &k, int dc_done) { return !dc_done && !k.done; }
+
+// Calls op(q, r) for the rows r < rows(q) of every system q with part(q):
+// the systems' row ranges, concatenated in system order, are cut
+// round-robin over the grid's threads (one system alone: thread t takes rows
+// t, t + threads, ...).
+template <int CAP, class Part, class Rows, class Op>
+__device__ __forceinline__ void mg_rows(const MSetArgT<CAP> &A, Part part, Rows rows, Op op) {
+    const long gtid = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    const long gth = (long)gridDim.x * blockDim.x;
+    long base = 0;
+    for (int q = 0; q < A.nsys; ++q) {
+        if (!part(q)) continue;
+        const int n = rows(q);
+        long first = gtid - base;  // smallest r >= 0 with base + r = gtid (mod gth)
+        if (first < 0) first += ((-first + gth - 1) / gth) * gth;
+        for (long r = first; r < n; r += gth) op(q, (int)r);
+        base += n;
+    }
+}
+
+// mg_apply for every system of a merged set that has a hierarchy and an
+// active inner solve (which = 0: y = M^-1 p, 1: z = M^-1 s).  Pass k of the
+// way down (or up) runs for the systems with more than k coarse levels, the
+// coarsest sweeps of system j in block j mod gridDim.x, so every system
+// takes exactly the steps and the arithmetic of mg_apply, with one set of
+// grid barriers for all of them.
+template <int CAP>
+__device__ bool mg_apply_set(const MSetArgT<CAP> &A, const KState *sst, const int *sdc, int which, GridBar *bar,
+                             unsigned int &target, int *s_ok) {
+    auto on = [&](int q) { return A.sys[q].mg.nlev > 0 && inner_active(sst[q], sdc[q]); };
+    auto lvl = [&](int q, int k) {
+        const MSys &S = A.sys[q];
+        return which == 0 ? mg_level(S, k, S.p, S.y) : mg_level(S, k, S.s, S.z);
+    };
+    int kmax = 0;
+    for (int q = 0; q < A.nsys; ++q)
+        if (on(q)) kmax = max(kmax, A.sys[q].mg.nlev);
+    for (int k = 0; k < kmax; ++k) {
+        auto part = [&](int q) { return on(q) && k < A.sys[q].mg.nlev; };
+        mg_rows(A, part, [&](int q) { return k == 0 ? A.sys[q].npad : A.sys[q].mg.lev[k].n; },
+                [&](int q, int r) {
+                    const MGView L = lvl(q, k);
+                    const float w = A.sys[q].mg.omega;
+                    L.x[r] = w * L.invdiag[r] * L.b[r];
+                });
+        if (!grid_sync(bar, target, s_ok)) return false;
+        mg_rows(A, part, [&](int q) { return k == 0 ? A.sys[q].n : A.sys[q].mg.lev[k].n; },
+                [&](int q, int r) {
+                    const MGView L = lvl(q, k);
+                    L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+                });
+        if (!grid_sync(bar, target, s_ok)) return false;
+        mg_rows(A, part, [&](int q) { return A.sys[q].mg.lev[k + 1].n; },
+                [&](int q, int I) {
+                    const MGView L = lvl(q, k);
+                    const MGLevel &C = A.sys[q].mg.lev[k + 1];
+                    float acc = 0.0f;
+                    for (int m = C.mstart[I]; m < C.mstart[I + 1]; ++m) acc += L.t[C.members[m]];
+                    C.b[I] = acc;
+                });
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    {
+        int j = 0;  // index of the system among those preconditioned
+        for (int q = 0; q < A.nsys; ++q) {
+            if (!on(q)) continue;
+            if (j++ % gridDim.x != blockIdx.x) continue;
+            const MGView L = lvl(q, A.sys[q].mg.nlev);
+            const float w = A.sys[q].mg.omega;
+            for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] = w * L.invdiag[r] * L.b[r];
+            __syncthreads();
+            for (int it = 0; it < A.sys[q].mg.sweeps; ++it) {
+                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+                __syncthreads();
+                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] += w * L.invdiag[r] * L.t[r];
+                __syncthreads();
+            }
+        }
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    for (int k = kmax - 1; k >= 0; --k) {
+        auto part = [&](int q) { return on(q) && k < A.sys[q].mg.nlev; };
+        auto rows = [&](int q) { return k == 0 ? A.sys[q].n : A.sys[q].mg.lev[k].n; };
+        mg_rows(A, part, rows, [&](int q, int r) {
+            const MGView L = lvl(q, k);
+            const MGLevel &C = A.sys[q].mg.lev[k + 1];
+            L.x[r] += C.x[C.agg[r]];
+        });
+        if (!grid_sync(bar, target, s_ok)) return false;
+        mg_rows(A, part, rows, [&](int q, int r) {
+            const MGView L = lvl(q, k);
+            L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+        });
+        if (!grid_sync(bar, target, s_ok)) return false;
+        mg_rows(A, part, rows, [&](int q, int r) {
+            const MGView L = lvl(q, k);
+            const float w = A.sys[q].mg.omega;
+            L.x[r] += w * L.invdiag[r] * L.t[r];
+        });
+        if (!grid_sync(bar, target, s_ok)) return false;
+    }
+    return true;
+}
+
+// y = M^-1 p (which = 0) or z = M^-1 s (1) for the multilevel systems of a set
+template <int CAP>
+__device__ __forceinline__ bool mg_precondition(const MSetArgT<CAP> &A, const KState *sst, const int *sdc,
+                                                int which, GridBar *bar, unsigned int &target, int *s_ok) {
+    if constexpr (CAP <= KMAX) {  // one solver instance's set: a single system
+        const MSys &S = A.sys[0];
+        return which == 0 ? mg_apply(S, S.p, S.y, bar, target, s_ok) : mg_apply(S, S.s, S.z, bar, target, s_ok);
+    } else {
+        return mg_apply_set(A, sst, sdc, which, bar, target, s_ok);
+    }
+}
+
 // Galerkin operator of a coarse level: per row, the sum of its block's
 // diagonal and internal couplings, and per direction the couplings that
 // leave the block (in the members' order)
@@ -395,13 +529,13 @@ __global__ void k_mg_galerkin(int npad_f, const int *__restrict__ nbr_f, const f
 // round of loads, and a small system spreads over 4x more groups.  Every
 // block keeps a copy of the inner state; the kernel ends when every inner
 // solve of the round is done or after `max_iters` iterations.
-__device__ __forceinline__ bool inner_active(const KState &k, int dc_done) { return !dc_done && !k.done; }
 
-template <bool FUSED>
+template <bool FUSED, int CAP>
 __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
-    k_m32_loop(const __grid_constant__ MSetArg A, GridBar *bar, int max_iters) {
-    __shared__ KState sst[KMAX];
-    __shared__ int sdc[KMAX];
+    k_m32_loop(const __grid_constant__ MSetArgT<CAP> A, GridBar *bar, int max_iters) {
+    static_assert(CAP <= LOOP_THREADS, "one thread copies each system's state");
+    __shared__ KState sst[CAP];
+    __shared__ int sdc[CAP];
     __shared__ double sm[LOOP_GROUPS][LANES];
     __shared__ int s_ok;
     const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
@@ -447,10 +581,11 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
-                if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+                if (lane == 0) sst[q].alpha = sst[q].rho / d;
             }
             __syncthreads();
             // B: s = r - alpha v', z = D^-1 s (stored for the own rows, recomputed
@@ -483,11 +618,12 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 double ftt, fts;
                 lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
-                if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+                if (lane == 0) sst[q].w = (ftt > 0.0) ? fts / ftt : 0.0;
             }
             __syncthreads();
             // C: x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
@@ -516,12 +652,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 double f0r, frr;
                 lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
                 if (lane == 0) {
-                    KState *st = &sst[gi];
+                    KState *st = &sst[q];
                     st->rr = frr;
                     st->iter += 1;
                     st->work += 1;
@@ -543,7 +680,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
         } else {
             // the preconditioner is multilevel for a single-system set with a
             // hierarchy (uniform across the grid: the scalars are per-block copies)
-            const bool mg_on = A.nsys == 1 && A.sys[0].mg.nlev > 0 && inner_active(sst[0], sdc[0]);
+            bool mg_on = false;
+            if constexpr (CAP <= KMAX) {
+                mg_on = A.nsys == 1 && A.sys[0].mg.nlev > 0 && inner_active(sst[0], sdc[0]);
+            } else {
+                for (int q = 0; q < A.nsys; ++q)
+                    mg_on = mg_on || (A.sys[q].mg.nlev > 0 && inner_active(sst[q], sdc[q]));
+            }
             // p = r + beta (p - w v); y = D^-1 p
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -561,7 +704,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             }
             if (!grid_sync(bar, target, &s_ok)) break;
             // multilevel preconditioning: y = M^-1 p (replaces the Jacobi y)
-            if (mg_on && !mg_apply(A.sys[0], A.sys[0].p, A.sys[0].y, bar, target, &s_ok)) break;
+            if (mg_on && !mg_precondition(A, sst, sdc, 0, bar, target, &s_ok)) break;
             // v = A y, <r0, v>
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -581,10 +724,11 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 if (lane == 0) S.part[4 * (size_t)S.nchunks * MSUB + lc] = (double)t;
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 const double d = lanes_final_sum(S.part + 4 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, 1, lane, sm[gi], gsync);
-                if (lane == 0) sst[gi].alpha = sst[gi].rho / d;
+                if (lane == 0) sst[q].alpha = sst[q].rho / d;
             }
             __syncthreads();
             // s = r - alpha v; z = D^-1 s
@@ -603,7 +747,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 }
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (mg_on && !mg_apply(A.sys[0], A.sys[0].s, A.sys[0].z, bar, target, &s_ok)) break;
+            if (mg_on && !mg_precondition(A, sst, sdc, 1, bar, target, &s_ok)) break;
             // t = A z, <t, t>, <t, s>
             for (int u = cbegin; u < total_units; u += gstride) {
                 const int si = msys_of_chunk(A, u / MSUB);
@@ -627,11 +771,12 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                 if (lane == 0) reinterpret_cast<double2 *>(S.part)[lc] = make_double2(tt, ts);
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 double ftt, fts;
                 lanes_final_sum2(S.part, S.nchunks * MSUB, lane, sm[gi], ftt, fts, gsync);
-                if (lane == 0) sst[gi].w = (ftt > 0.0) ? fts / ftt : 0.0;
+                if (lane == 0) sst[q].w = (ftt > 0.0) ? fts / ftt : 0.0;
             }
             __syncthreads();
             // x += alpha y + w z; r = s - w t; <r0, r>, <r, r>
@@ -660,12 +805,13 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     reinterpret_cast<double2 *>(S.part + 2 * (size_t)S.nchunks * MSUB)[lc] = make_double2(t0r, trr);
             }
             if (!grid_sync(bar, target, &s_ok)) break;
-            if (gi < A.nsys && inner_active(sst[gi], sdc[gi])) {
-                const MSys &S = A.sys[gi];
+            for (int q = gi; q < A.nsys; q += LOOP_GROUPS) {
+                if (!inner_active(sst[q], sdc[q])) continue;
+                const MSys &S = A.sys[q];
                 double f0r, frr;
                 lanes_final_sum2(S.part + 2 * (size_t)S.nchunks * MSUB, S.nchunks * MSUB, lane, sm[gi], f0r, frr, gsync);
                 if (lane == 0) {
-                    KState *st = &sst[gi];
+                    KState *st = &sst[q];
                     st->rr = frr;
                     st->iter += 1;
                     st->work += 1;
@@ -686,7 +832,12 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             __syncthreads();
         }
         bool any = false;
-        for (int q = 0; q < A.nsys; ++q) any = any || inner_active(sst[q], sdc[q]);
+        if constexpr (CAP <= KMAX) {
+            for (int q = 0; q < A.nsys; ++q) any = any || inner_active(sst[q], sdc[q]);
+        } else {  // the lanes of each warp split the systems
+            for (int q = threadIdx.x & 31; q < A.nsys; q += 32) any = any || inner_active(sst[q], sdc[q]);
+            any = __any_sync(0xffffffffu, any);
+        }
         if (!any) {
             ++it;
             break;
@@ -704,7 +855,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
 // residual along delta, so a correction from an inaccurate FP32 solve can
 // shrink the residual less but never grow it.  The last block to finish
 // sets dc->theta.
-__global__ void __launch_bounds__(LANES) k_dc_step(const __grid_constant__ MSetArg A) {
+template <int CAP>
+__global__ void __launch_bounds__(LANES) k_dc_step(const __grid_constant__ MSetArgT<CAP> A) {
     __shared__ double sm[LANES];
     __shared__ int sh[4];
     for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
@@ -743,7 +895,8 @@ __global__ void __launch_bounds__(LANES) k_dc_step(const __grid_constant__ MSetA
     }
 }
 
-__global__ void k_dc_update(const __grid_constant__ MSetArg A) {
+template <int CAP>
+__global__ void k_dc_update(const __grid_constant__ MSetArgT<CAP> A) {
     for (int c = blockIdx.x; c < A.total_chunks; c += gridDim.x) {
         const MSys &S = A.sys[msys_of_chunk(A, c)];
         if (!(__ldcg(&S.dc->done) == 0 && __ldcg(&S.st->info) == 0)) continue;
@@ -792,20 +945,22 @@ void launch_to_f32(const double *coef, const double *invdiag, int npad, float *c
                                                                                 invdiag32);
 }
 
-void launch_dc_resid(const MSetArg &A, int first, cudaStream_t st) {
+template <int CAP>
+void launch_dc_resid(const MSetArgT<CAP> &A, int first, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_dc_resid<<<m_grid(A.total_chunks), LANES, 0, st>>>(A, first);
+    k_dc_resid<CAP><<<m_grid(A.total_chunks), LANES, 0, st>>>(A, first);
     if (first) {
         count_launches(1);
-        k_dc_zero<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
+        k_dc_zero<CAP><<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
     }
 }
 
-void launch_m32_init(const MSetArg &A, cudaStream_t st) {
+template <int CAP>
+void launch_m32_init(const MSetArgT<CAP> &A, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
     count_launches(1);
-    k_m32_init<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_m32_init<CAP><<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
 
 
@@ -814,9 +969,12 @@ void launch_m32_init(const MSetArg &A, cudaStream_t st) {
 // five-phase loop, whose smaller working set stays in the L2 (measured: a
 // 42 K-row solve 9% faster fused, a 1 M-row solve 16% slower).
 constexpr long kFusedRows = 1L << 19;
-static std::atomic<int> g_m32_occ[2];
 
-cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaStream_t st) {
+// (the V-cycle runs in the five-phase loop)
+bool m32_fused(long rows, bool mg) { return rows <= kFusedRows && !mg; }
+
+template <int CAP>
+cudaError_t launch_m32_loop(const MSetArgT<CAP> &A, GridBar *bar, int max_iters, cudaStream_t st, int variant) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
     long rows = 0;
     bool mg = false;
@@ -824,29 +982,42 @@ cudaError_t launch_m32_loop(const MSetArg &A, GridBar *bar, int max_iters, cudaS
         rows += A.sys[i].n;
         mg = mg || A.sys[i].mg.nlev > 0;
     }
-    const bool fused = rows <= kFusedRows && !mg;  // the V-cycle runs in the five-phase loop
-    const void *fn = fused ? (const void *)k_m32_loop<true> : (const void *)k_m32_loop<false>;
-    int occ = g_m32_occ[fused].load();
+    const bool fused = variant < 0 ? m32_fused(rows, mg) : (variant == 1 && !mg);
+    const void *fn = fused ? (const void *)k_m32_loop<true, CAP> : (const void *)k_m32_loop<false, CAP>;
+    static std::atomic<int> occ_cache[2];
+    int occ = occ_cache[fused].load();
     if (occ == 0) {
         cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, LOOP_THREADS, 0);
         if (e != cudaSuccess) return e;
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
-        g_m32_occ[fused] = occ;
+        occ_cache[fused] = occ;
     }
-    const int grid = loop_grid(A.total_chunks * MSUB, MSUB, occ);
+    // a merged set (many solves' systems) spreads over every SM
+    const int grid = CAP > KMAX ? std::max(1, std::min(A.total_chunks * MSUB, device_sm_count() * occ))
+                                : loop_grid(A.total_chunks * MSUB, MSUB, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
-    MSetArg a = A;
+    MSetArgT<CAP> a = A;
     void *args[] = {&a, &bar, &max_iters};
     count_launches(1);
     return cudaLaunchCooperativeKernel(fn, grid, LOOP_THREADS, args, 0, st);
 }
 
-void launch_dc_update(const MSetArg &A, cudaStream_t st) {
+template <int CAP>
+void launch_dc_update(const MSetArgT<CAP> &A, cudaStream_t st) {
     if (A.total_chunks <= 0) return;
     count_launches(2);
-    k_dc_step<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
-    k_dc_update<<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_dc_step<CAP><<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
+    k_dc_update<CAP><<<m_grid(A.total_chunks), LANES, 0, st>>>(A);
 }
+
+template void launch_dc_resid<KMAX>(const MSetArg &, int, cudaStream_t);
+template void launch_dc_resid<KMAX_MERGED_M>(const MSetArgMerged &, int, cudaStream_t);
+template void launch_m32_init<KMAX>(const MSetArg &, cudaStream_t);
+template void launch_m32_init<KMAX_MERGED_M>(const MSetArgMerged &, cudaStream_t);
+template cudaError_t launch_m32_loop<KMAX>(const MSetArg &, GridBar *, int, cudaStream_t, int);
+template cudaError_t launch_m32_loop<KMAX_MERGED_M>(const MSetArgMerged &, GridBar *, int, cudaStream_t, int);
+template void launch_dc_update<KMAX>(const MSetArg &, cudaStream_t);
+template void launch_dc_update<KMAX_MERGED_M>(const MSetArgMerged &, cudaStream_t);
 
 }  // namespace ns3d

@@ -60,22 +60,40 @@ struct MSys {
     MGSet mg;
 };
 
-// A mixed solve set as a kernel argument (by value; systems in chunk order)
-struct MSetArg {
+// A mixed solve set as a kernel argument (by value; systems in chunk order):
+// one solver instance's systems (up to KMAX) or the systems of many
+// concurrent solves (up to KMAX_MERGED_M, 24 KB of kernel parameters).
+constexpr int KMAX_MERGED_M = 32;
+template <int CAP>
+struct MSetArgT {
     int nsys, total_chunks;
-    MSys sys[KMAX];
+    MSys sys[CAP];
 };
+using MSetArg = MSetArgT<KMAX>;
+using MSetArgMerged = MSetArgT<KMAX_MERGED_M>;
+static_assert(sizeof(MSetArgMerged) <= 32000, "kernel parameter space");
 
 // Galerkin operators of every coarse level of `mg` from the FP32 system
 void launch_mg_galerkin(const MSys &sys, cudaStream_t st);
 void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
                    cudaStream_t st);
-void launch_dc_resid(const MSetArg &set, int first, cudaStream_t st);
-void launch_m32_init(const MSetArg &set, cudaStream_t st);
+// (the set launchers are instantiated for CAP = KMAX and KMAX_MERGED_M)
+template <int CAP>
+void launch_dc_resid(const MSetArgT<CAP> &set, int first, cudaStream_t st);
+template <int CAP>
+void launch_m32_init(const MSetArgT<CAP> &set, cudaStream_t st);
+// The FP32 loop variant of a set: fused (three phases per iteration) when
+// the set has at most kFusedRows rows and no multilevel system, else the
+// five-phase loop.  A merged set runs the variant its members chose alone.
+bool m32_fused(long rows, bool mg);
 // FP32 inner iterations until every inner solve of the round is done
-cudaError_t launch_m32_loop(const MSetArg &set, GridBar *bar, int max_iters, cudaStream_t st);
+// (variant: -1 from the set's own rows, 0 five-phase, 1 fused)
+template <int CAP>
+cudaError_t launch_m32_loop(const MSetArgT<CAP> &set, GridBar *bar, int max_iters, cudaStream_t st,
+                            int variant = -1);
 // theta = <r, A d> / <A d, A d> for the FP32 correction d (FP64 SpMV), then
 // x += theta d
-void launch_dc_update(const MSetArg &set, cudaStream_t st);
+template <int CAP>
+void launch_dc_update(const MSetArgT<CAP> &set, cudaStream_t st);
 
 }  // namespace ns3d

@@ -93,16 +93,19 @@ static void build_mg(DevSys &S, cudaStream_t st) {
     S.mg = std::move(H);
 }
 
-void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
+template <int CAP>
+void MixedSetT<CAP>::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     std::vector<const double *> key;
     for (const SolveItem &it : items) {
         key.push_back(it.sys->coef.p);
         key.push_back(it.x);
         key.push_back(it.b);
     }
-    if (key == key_) return;
+    // a merged set's members come and go (a new solve may reuse a finished
+    // one's addresses): it is set up afresh every run
+    if (CAP <= KMAX && key == key_) return;
     const int ns = (int)items.size();
-    if (ns > KMAX) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
+    if (ns > CAP) throw ApiError(NS3D_ERR_ARG, "too many systems in one solve set");
     std::vector<MSys> ms(ns);
     int chunk = 0;
     if (!bar_.n) {
@@ -140,7 +143,11 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
         m.part = S.part.p;
         m.st = st_.p + i;
         m.dc = dc_.p + i;
-        if (use_mg && ns == 1 && S.n > kMGCoarsest && S.cell_ny > 0) {
+        // a solver instance's own set: the multilevel preconditioner for a
+        // single system; a merged set: what each system's own set chose
+        const bool mg = CAP > KMAX ? (items[i].mg && S.mg)
+                                   : (use_mg && ns == 1 && S.n > kMGCoarsest && S.cell_ny > 0);
+        if (mg) {
             if (!S.mg) build_mg(S, st);
             m.mg.nlev = S.mg->nlev;
             m.mg.sweeps = 30;
@@ -172,7 +179,20 @@ void MixedSet::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     total_chunks_ = chunk;
 }
 
-void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out) {
+template <int CAP>
+int MixedSetT<CAP>::variant() const {
+    long rows = 0;
+    bool mg = false;
+    for (int i = 0; i < nsys_; ++i) {
+        rows += set_.sys[i].n;
+        mg = mg || set_.sys[i].mg.nlev > 0;
+    }
+    return m32_fused(rows, mg) ? 1 : 0;
+}
+
+template <int CAP>
+void MixedSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out,
+                         int variant) {
     configure(items, st);
     const int ns = nsys_;
     int maxit = 0;
@@ -220,7 +240,7 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
         if (all_done) break;
         if (++rounds > maxit + 2L) throw ApiError(NS3D_ERR_TIMEOUT, "defect correction exceeded its round bound");
         launch_m32_init(set_, st);
-        NS3D_CUDA_CHECK(launch_m32_loop(set_, bar_.p, maxit + 64, st));
+        NS3D_CUDA_CHECK(launch_m32_loop(set_, bar_.p, maxit + 64, st, variant));
         launch_dc_update(set_, st);
         launch_dc_resid(set_, 0, st);
     }
@@ -243,5 +263,8 @@ void MixedSet::run(const std::vector<SolveItem> &items, cudaStream_t st, std::ve
     }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(out_st_.p, h_out_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
 }
+
+template class MixedSetT<KMAX>;
+template class MixedSetT<KMAX_MERGED_M>;
 
 }  // namespace ns3d

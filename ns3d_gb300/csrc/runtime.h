@@ -143,6 +143,7 @@ struct SolveItem {
     const double *b;  // right-hand side (npad doubles)
     double tol;
     int maxit;
+    bool mg = false;  // merged mixed sets: the system's own set chose the multilevel preconditioner
 };
 
 struct SolveOutcome {
@@ -205,50 +206,6 @@ class KrylovSetT {
 using KrylovSet = KrylovSetT<KMAX>;
 using KrylovSetMerged = KrylovSetT<KMAX_MERGED>;
 
-// The FP64 solves of many concurrent solver instances merged into one set of
-// persistent kernels: each member's BiCGSTAB sets (its momentum components,
-// its pressure system) are queued here, and one member at a time (the
-// leader) gathers every queued set, up to KMAX_MERGED systems, and solves
-// them with one loop launch per round over the ragged list of their
-// 1024-row chunks, on the group's own stream.  The leader waits for the
-// other members up to a short window (the members run their outer
-// iterations in near lockstep), so the launches stay full.  Each system
-// keeps its own scalars and reduction order, so a solve gives the same bits
-// alone and merged.
-class SolveGroup {
-  public:
-    SolveGroup();
-    ~SolveGroup();
-    // a solve of a member starts / ends (the leader waits for members only)
-    void join();
-    void leave();
-    // Solves `items` (whose inputs are ready on `st`) with whatever else the
-    // members queue meanwhile.  On return `out` holds the outcomes, the
-    // final state of item i is in state_dst[i] (device), and work queued on
-    // `st` afterwards runs after the merged launch.
-    void run(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
-             std::vector<SolveOutcome> &out);
-    struct Stats {
-        int64_t launches = 0, requests = 0, systems = 0;
-        int max_systems = 0, max_requests = 0;
-    };
-    Stats stats();
-    double window_s = 2e-3;  // longest wait of a leader for the other members
-
-  private:
-    struct Req;
-    void execute(std::vector<Req *> &batch);
-    std::mutex mu_;
-    std::condition_variable cv_;
-    std::deque<Req *> pending_;
-    int members_ = 0;
-    bool leading_ = false;
-    Stats stats_;
-    cudaStream_t stream_ = nullptr;
-    std::unique_ptr<KrylovSetMerged> set_;
-};
-// the solve group behind a C-ABI group handle (NULL for NULL)
-SolveGroup *group_of(ns3d_group *g);
 
 struct DCState;
 
@@ -261,17 +218,29 @@ struct DCState;
 
 // A set of systems solved by FP32 BiCGSTAB inside FP64 defect correction.
 // The FP32 copy of each matrix is refreshed from the FP64 one at every run.
-class MixedSet {
+// MixedSet: one solver instance's systems; MixedSetMerged: the systems of
+// many concurrent solves (SolveGroup), each with the preconditioner and FP32
+// loop variant its own set chose.
+template <int CAP>
+class MixedSetT {
   public:
-    void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out);
+    // variant: -1 from the set's own rows, 0 five-phase, 1 fused FP32 loop
+    void run(const std::vector<SolveItem> &items, cudaStream_t st, std::vector<SolveOutcome> &out,
+             int variant = -1);
     const KState *inner_state(int i) const { return st_.p + i; }
     // FP64 outcome of system i, mirrored into a KState (iter, info) for the
     // velocity post-processing kernel
     const KState *device_state(int i) const { return out_st_.p + i; }
+    // set-up without solving (FP32 buffers, hierarchy, state buffers): a
+    // merged run solves these items and leaves the outcome states here
+    void prepare(const std::vector<SolveItem> &items, cudaStream_t st) { configure(items, st); }
+    KState *out_state_buffer() { return out_st_.p; }
+    bool uses_mg(int i) const { return set_.sys[i].mg.nlev > 0; }
+    int variant() const;  // the FP32 loop variant this set runs (0 five-phase, 1 fused)
     bool use_mg = false;                          // multilevel preconditioner for single-system sets
     double inner_rel_tol = NS3D_MIXED_INNER_TOL;  // floor of the per-round FP32 reduction target
     int inner_cap = NS3D_MIXED_INNER_CAP;         // FP32 iterations per round at most
-    ~MixedSet() = default;
+    ~MixedSetT() = default;
 
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
@@ -280,10 +249,65 @@ class MixedSet {
     HBuf<KState> h_st_, h_out_;
     HBuf<DCState> h_dc_;
     std::vector<const double *> key_;
-    MSetArg set_;  // passed to every kernel by value
+    MSetArgT<CAP> set_;  // passed to every kernel by value
     DBuf<GridBar> bar_;
     HBuf<int> h_err_;
     int nsys_ = 0, total_chunks_ = 0;
 };
+using MixedSet = MixedSetT<KMAX>;
+using MixedSetMerged = MixedSetT<KMAX_MERGED_M>;
+
+// The BiCGSTAB work of many concurrent solver instances merged into shared
+// persistent kernels: each member's solve sets (its momentum components,
+// its pressure system; FP64, or FP32 inside FP64 defect correction) are
+// queued here, and one member at a time (the leader) gathers the queued sets
+// of one kind -- FP64, or mixed precision with one FP32 loop variant -- up to
+// KMAX_MERGED (FP64) or KMAX_MERGED_M (mixed) systems, and solves them
+// together on the group's own stream: every launch covers the ragged list of
+// all their 1024-row chunks.  The leader waits for the other members up to a
+// short window (the members run their outer iterations in near lockstep),
+// so the launches stay full.  Each system keeps its own scalars, reduction
+// order and preconditioner, so a solve gives the same bits alone and merged.
+class SolveGroup {
+  public:
+    SolveGroup();
+    ~SolveGroup();
+    // a solve of a member starts / ends (the leader waits for members only)
+    void join();
+    void leave();
+    // Solves the FP64 set `items` (whose inputs are ready on `st`) with
+    // whatever else the members queue meanwhile.  On return `out` holds the
+    // outcomes, the final state of item i is in state_dst[i] (device), and
+    // work queued on `st` afterwards runs after the merged launches.
+    void run(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
+             std::vector<SolveOutcome> &out);
+    // The same for a mixed-precision set (its items carry their
+    // preconditioner choice; variant: the set's FP32 loop variant); the
+    // outcome state of item i (MixedSet::device_state) lands in state_dst[i].
+    void run_mixed(const std::vector<SolveItem> &items, cudaStream_t st, KState *state_dst,
+                   std::vector<SolveOutcome> &out, int variant);
+    struct Stats {
+        int64_t launches = 0, requests = 0, systems = 0;
+        int max_systems = 0, max_requests = 0;
+    };
+    Stats stats();
+    double window_s = 2e-3;  // longest wait of a leader for the other members
+
+  private:
+    struct Req;
+    void submit(Req &r);
+    void execute(std::vector<Req *> &batch);
+    std::mutex mu_;
+    std::condition_variable cv_;
+    std::deque<Req *> pending_;
+    int members_ = 0;
+    bool leading_ = false;
+    Stats stats_;
+    cudaStream_t stream_ = nullptr;
+    std::unique_ptr<KrylovSetMerged> set_;
+    std::unique_ptr<MixedSetMerged> mset_;
+};
+// the solve group behind a C-ABI group handle (NULL for NULL)
+SolveGroup *group_of(ns3d_group *g);
 
 }  // namespace ns3d

@@ -262,7 +262,7 @@ struct ns3d_handle {
     HBuf<DiagOut> h_diag;
     KrylovSet kmom, kp;
     MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
-    SolveGroup *group = nullptr;  // FP64 sets merged with other solves' (ns3d_set_group)
+    SolveGroup *group = nullptr;  // sets merged with other solves' (ns3d_set_group)
     bool mixed() const { return prm.precision != NS3D_FP64; }
     // an FP64 set: alone, or merged with the sets of the group's other solves
     void run_fp64(KrylovSet &own, const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
@@ -273,8 +273,19 @@ struct ns3d_handle {
         own.prepare(items, stream);  // the merged run leaves the final states here
         group->run(items, stream, own.state_buffer(), out);
     }
+    // a mixed-precision set: alone, or merged (with the preconditioner and
+    // FP32 loop variant its own set chooses)
+    void run_mixed(MixedSet &own, std::vector<SolveItem> items, std::vector<SolveOutcome> &out) {
+        if (!group) {
+            own.run(items, stream, out);
+            return;
+        }
+        own.prepare(items, stream);  // FP32 copies, hierarchy, outcome states
+        for (size_t i = 0; i < items.size(); ++i) items[i].mg = own.uses_mg((int)i);
+        group->run_mixed(items, stream, own.out_state_buffer(), out, own.variant());
+    }
     void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
-        if (mixed()) mp.run(items, stream, out);
+        if (mixed()) run_mixed(mp, items, out);
         else run_fp64(kp, items, out);
     }
 
@@ -456,7 +467,7 @@ void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
                                     {&V, v.p, V.rhs.p, prm.vsolvertol, prm.maxitsolver}};
     if (nw > 0) items.push_back({&W, w.p, W.rhs.p, prm.vsolvertol, prm.maxitsolver});
     std::vector<SolveOutcome> out;
-    if (mixed()) mmom.run(items, stream, out);
+    if (mixed()) run_mixed(mmom, items, out);
     else run_fp64(kmom, items, out);
     auto state = [&](int i) { return mixed() ? mmom.device_state(i) : kmom.device_state(i); };
     launch_velocity_post(utemp.p, u.p, nu, state(0), limit, dvmax, stream);
@@ -1075,7 +1086,7 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
         ~Member() {
             if (g) g->leave();
         }
-    } member(h.mixed() ? nullptr : h.group);
+    } member(h.group);
     if (h.prm.method == NS3D_SIMPLEC) h.run_simplec();
     else h.run_simpler_family(h.prm.method);
     return NS3D_OK;

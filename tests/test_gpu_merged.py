@@ -1,8 +1,8 @@
-"""Merged solve sets: the FP64 BiCGSTAB sets of concurrent solves of
-different images (sizes, flow directions, methods) run together in shared
-persistent loop-kernel launches over a ragged list of chunks, and every solve
-gives exactly the result it gives alone (bit-identical fields, K and
-iteration counts)."""
+"""Merged solve sets: the BiCGSTAB sets (FP64, or FP32 inside FP64 defect
+correction) of concurrent solves of different images (sizes, flow
+directions, methods) run together in shared persistent loop-kernel launches
+over a ragged list of chunks, and every solve gives exactly the result it
+gives alone (bit-identical fields, K and iteration counts)."""
 import threading
 
 import numpy as np
@@ -37,11 +37,13 @@ def _alone(lib, reqs):
     return out
 
 
-def test_group_solves_equal_alone(gpulib):
-    reqs = _requests(gpulib)
-    alone = _alone(gpulib, reqs)
-    group = capi.Group(gpulib)
-    solvers = [capi.Solver(gpulib, p, synth.to_raw(img), img.shape) for p, img in reqs]
+def _group_solve_and_compare(lib, reqs):
+    """Solves every request alone, then all of them at once on their own
+    threads with their solvers attached to one group; asserts bit-identical
+    results and returns the group's statistics."""
+    alone = _alone(lib, reqs)
+    group = capi.Group(lib)
+    solvers = [capi.Solver(lib, p, synth.to_raw(img), img.shape) for p, img in reqs]
     for s in solvers:
         group.attach(s)
     results = [None] * len(solvers)
@@ -67,6 +69,11 @@ def test_group_solves_equal_alone(gpulib):
     for s in solvers:
         s.close()
     group.destroy()
+    return st
+
+
+def test_group_solves_equal_alone(gpulib):
+    st = _group_solve_and_compare(gpulib, _requests(gpulib))
     # the sets were really merged: some launches served several solves
     assert st.launches > 0 and st.max_requests >= 2
     assert st.systems > st.launches
@@ -109,18 +116,15 @@ def test_merged_batch_and_server_match_single_solves(gpulib):
     assert gs.launches > 0 and gs.requests >= len(reqs)
 
 
-def test_mixed_precision_requests_ignore_the_group(gpulib):
-    """Mixed-precision solves run their own sets (the group serves FP64 only)
-    and still give their stand-alone result inside a merging server."""
-    shape, r_, phi, direction, method = SPECS[0]
-    img, _ = synth.rsa_spheres(shape, r_, phi, seed=70)
-    p = params(gpulib, method=method, direction=direction, maxitSIMPLE=80, simpletol=1e-5, precision=1)
-    s = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
-    k = s.solve().K
-    s.close()
-    srv = capi.Server(gpulib, max_active=2, merge=True)
-    t = srv.submit(p, synth.to_raw(img), img.shape)
-    r, _ = srv.wait(t)
-    gs = srv.group_stats()
-    srv.stop()
-    assert r.K == k and gs.launches == 0
+@pytest.mark.parametrize("precision", [1, 2], ids=["mixed", "mixed_mg"])
+def test_mixed_precision_group_solves_equal_alone(gpulib, precision):
+    """FP32-inner solves merge too (with the multilevel preconditioner of
+    precision 2 applied per system inside the shared launch) and each gives
+    its stand-alone result, bit for bit."""
+    reqs = []
+    for k, (shape, r_, phi, direction, method) in enumerate(SPECS[:4]):
+        img, _ = synth.rsa_spheres(shape, r_, phi, seed=90 + k)
+        reqs.append((params(gpulib, method=method, direction=direction, maxitSIMPLE=60, simpletol=1e-5,
+                            precision=precision), img))
+    st = _group_solve_and_compare(gpulib, reqs)
+    assert st.launches > 0 and st.max_requests >= 2
