@@ -370,6 +370,7 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
 # trajectory bit for bit (fixed-order reductions), so max_outer may cap the
 # outer iterations of every leg alike.
 MERGED_IMAGES = 16
+MERGED_LANES = (1, 2)  # lanes of the solve group (cohorts of ceil(solves / lanes))
 
 
 def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
@@ -404,9 +405,13 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
                                          "cell_updates_per_s": cells / t1,
                                          "bicgstab_row_iterations_per_s": rows / t1}}
     mixed = "mixed_mg" if SERVE_PRECISION == 2 else "mixed"
-    for name, merged, precision in (("batch_fp64_streams", False, 0), ("batch_fp64_merged", True, 0),
-                                    ("batch_%s_streams" % mixed, False, SERVE_PRECISION),
-                                    ("batch_%s_merged" % mixed, True, SERVE_PRECISION)):
+    legs_spec = []
+    for precision, label in ((0, "fp64"), (SERVE_PRECISION, mixed)):
+        legs_spec.append(("batch_%s_streams" % label, 0, precision))
+        for lanes in MERGED_LANES:
+            legs_spec.append(("batch_%s_merged_%d_lane%s" % (label, lanes, "s" if lanes > 1 else ""), lanes,
+                              precision))
+    for name, merged, precision in legs_spec:
         t = time.perf_counter()
         res, status, g, rc = capi.batch_solve(lib, [prm(r, precision) for r in imgs], [r["raw"] for r in imgs],
                                               [r["shape"] for r in imgs], max_concurrent, merged=merged)
@@ -420,9 +425,11 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
             leg["max_K_rel_err_vs_fp64"] = max(abs(x.K - k) / abs(k) for x, k in zip(res, k1))
             leg["outer_iterations"] = [int(x.iterations) for x in res]
         if g is not None:
+            leg["lanes"] = merged
             leg["group"] = g.as_dict()
             leg["mean_systems_per_set"] = g.systems / max(g.launches, 1)
         legs[name] = leg
+    legs["autotune_table"] = capi.autotune_table(lib).splitlines()
     legs["workload"] = ("%d images, edges from %s per axis, sphere (r 3-8, phi 0.35-0.9, overlapping) or fibre "
                         "(r 2-4, phi 0.7-0.95) packs generated on the device, SIMPLEC, flow x, plain FP64, "
                         "at most %d outer iterations" % (n_images, edges, max_outer))

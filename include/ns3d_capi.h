@@ -342,14 +342,16 @@ NS3D_API int ns3d_server_stop(ns3d_server *s);
  * Merged solve sets (no counterpart in the reference, which solves one image
  * per process with Eigen, src/NSBase.cxx:1799,1825,1852,2343,2393,2397).
  * Solver instances attached to one group pool their FP64 BiCGSTAB sets (the
- * three momentum components, the pressure(-correction) system) while they
- * solve: one persistent loop-kernel launch per round serves up to 64 systems
- * of many images of different sizes, laid out as one ragged list of 1024-row
- * chunks.  Every system keeps its own Krylov scalars and reduction order, so
- * each result is bit-identical to the solve alone.  Mixed-precision solves
- * ignore the group.  Attach with ns3d_set_group before ns3d_solve (NULL
- * detaches); destroy a group only after every solve attached to it returned.
- * The solves of a group must run on separate host threads.
+ * three momentum components, the pressure(-correction) system; FP64, or FP32
+ * inside FP64 defect correction) while they solve: one persistent
+ * loop-kernel launch per round serves up to 64 FP64 (32 mixed) systems of
+ * many images of different sizes, laid out as one ragged list of 1024-row
+ * chunks.  Every system keeps its own Krylov scalars, reduction order and
+ * preconditioner, so each result is bit-identical to the solve alone.
+ * Attach with ns3d_set_group before ns3d_solve (NULL detaches); destroy a
+ * group only after every solve attached to it returned and every handle
+ * that was attached to it was closed.  The solves of a group must run on
+ * separate host threads.
  */
 typedef struct ns3d_group ns3d_group;
 typedef struct ns3d_group_stats {
@@ -358,17 +360,33 @@ typedef struct ns3d_group_stats {
     int64_t systems;   /* linear systems they solved */
     int32_t max_systems, max_requests;  /* the largest merged set */
 } ns3d_group_stats;
-NS3D_API int ns3d_group_create(ns3d_group **out);
+/* lanes (1-16): merged solves that may run at once, each for a cohort of
+ * about members / lanes solves */
+NS3D_API int ns3d_group_create(int32_t lanes, ns3d_group **out);
 NS3D_API int ns3d_set_group(ns3d_handle *h, ns3d_group *g);
 NS3D_API int ns3d_group_get_stats(ns3d_group *g, ns3d_group_stats *out);
 NS3D_API int ns3d_group_destroy(ns3d_group *g);
-/* every FP64 request of the server solves in one group (before the first submit) */
-NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t enable);
+/* lanes > 0: every request of the server solves in one group of that many
+ * lanes; 0: no merging (before the first submit) */
+NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t lanes);
 NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out);
-/* ns3d_batch_solve with the FP64 solves merged; stats (may be NULL) of the group */
+/*
+ * Autotuner of merged solve sets (no counterpart in the reference).  The
+ * persistent loop kernel of a merged set may run on any number of blocks
+ * without changing a bit of the results (fixed-order reductions); the
+ * library times each candidate grid (the base grid / 1, 2, 4, 8) on three
+ * live launches per class of set (solver kind, size, lanes) and then keeps
+ * the fastest per row-iteration.  mode 0: off (base grid), 1: on (default),
+ * 2: on with the measurements forgotten.  The table (one line per class;
+ * `cap` bytes with the terminating zero) returns its full length.
+ */
+NS3D_API int ns3d_autotune_enable(int32_t mode);
+NS3D_API int ns3d_autotune_table(char *buf, int32_t cap);
+/* ns3d_batch_solve with the solves merged in a group of `lanes` lanes;
+ * stats (may be NULL) of the group */
 NS3D_API int ns3d_batch_solve_merged(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
-                                     int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status,
-                                     ns3d_group_stats *stats);
+                                     int32_t njobs, int32_t max_concurrent, int32_t lanes, ns3d_result *results,
+                                     int32_t *status, ns3d_group_stats *stats);
 
 /* ---- host utilities (CUDA library only; no device work) ----------------- */
 /*

@@ -289,13 +289,15 @@ def _declare_server(lib):
         "ns3d_batch_solve": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32, _P(Result),
                                        _i32]),
         "ns3d_batch_solve_merged": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, C.c_int32,
-                                              _P(Result), _i32, _P(GroupStats)]),
+                                              C.c_int32, _P(Result), _i32, _P(GroupStats)]),
         "ns3d_server_set_merging": (C.c_int, [C.c_void_p, C.c_int32]),
         "ns3d_server_group_stats": (C.c_int, [C.c_void_p, _P(GroupStats)]),
-        "ns3d_group_create": (C.c_int, [_P(C.c_void_p)]),
+        "ns3d_group_create": (C.c_int, [C.c_int32, _P(C.c_void_p)]),
         "ns3d_set_group": (C.c_int, [C.c_void_p, C.c_void_p]),
         "ns3d_group_get_stats": (C.c_int, [C.c_void_p, _P(GroupStats)]),
         "ns3d_group_destroy": (C.c_int, [C.c_void_p]),
+        "ns3d_autotune_enable": (C.c_int, [C.c_int32]),
+        "ns3d_autotune_table": (C.c_int, [C.c_char_p, C.c_int32]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -308,7 +310,8 @@ def _declare_server(lib):
 class Server:
     """Continuous-batching solve server (ns3d_server_*)."""
 
-    def __init__(self, lib, max_active, hbm_budget_bytes=0, merge=False):
+    def __init__(self, lib, max_active, hbm_budget_bytes=0, merge=0):
+        """merge: 0 no merging, n > 0 merged solve sets in a group of n lanes"""
         self.lib = _declare_server(lib)
         h = C.c_void_p()
         rc = self.lib.ns3d_server_start(int(max_active), int(hbm_budget_bytes), C.byref(h))
@@ -317,7 +320,7 @@ class Server:
         self.h = h
         self.sizes = {}
         if merge:
-            rc = self.lib.ns3d_server_set_merging(self.h, 1)
+            rc = self.lib.ns3d_server_set_merging(self.h, int(merge))
             if rc != 0:
                 raise NS3DError(rc, "merging unavailable")
 
@@ -404,10 +407,10 @@ class Group:
     their FP64 BiCGSTAB sets into shared persistent launches while they solve
     on separate host threads."""
 
-    def __init__(self, lib):
+    def __init__(self, lib, lanes=1):
         self.lib = _declare_server(lib)
         h = C.c_void_p()
-        rc = self.lib.ns3d_group_create(C.byref(h))
+        rc = self.lib.ns3d_group_create(int(lanes), C.byref(h))
         if rc != 0:
             raise NS3DError(rc, lib.ns3d_last_error().decode())
         self.h = h
@@ -428,8 +431,8 @@ class Group:
             self.h = None
 
 
-def batch_solve(lib, params_list, images_xfastest, dims_list, max_concurrent, merged=False):
-    """ns3d_batch_solve / ns3d_batch_solve_merged over host images.
+def batch_solve(lib, params_list, images_xfastest, dims_list, max_concurrent, merged=0):
+    """ns3d_batch_solve / ns3d_batch_solve_merged (merged = lanes > 0) over host images.
     Returns (results, statuses, group stats or None, return code)."""
     lib = _declare_server(lib)
     n = len(params_list)
@@ -441,9 +444,18 @@ def batch_solve(lib, params_list, images_xfastest, dims_list, max_concurrent, me
     st = np.zeros(n, np.int32)
     if merged:
         g = GroupStats()
-        rc = lib.ns3d_batch_solve_merged(ps, ptrs, _ptr(dims, C.c_int32), n, int(max_concurrent), res,
-                                         _ptr(st, C.c_int32), C.byref(g))
+        rc = lib.ns3d_batch_solve_merged(ps, ptrs, _ptr(dims, C.c_int32), n, int(max_concurrent), int(merged),
+                                         res, _ptr(st, C.c_int32), C.byref(g))
     else:
         g = None
         rc = lib.ns3d_batch_solve(ps, ptrs, _ptr(dims, C.c_int32), n, int(max_concurrent), res, _ptr(st, C.c_int32))
     return list(res), st, g, rc
+
+
+def autotune_table(lib):
+    """The merged-set grid autotuner's table (ns3d_autotune_table), one line
+    per class of set."""
+    lib = _declare_server(lib)
+    buf = C.create_string_buffer(1 << 16)
+    lib.ns3d_autotune_table(buf, len(buf))
+    return buf.value.decode()

@@ -31,16 +31,26 @@ struct SolveGroup::Req {
     std::string err;
 };
 
-SolveGroup::SolveGroup() : set_(new KrylovSetMerged()), mset_(new MixedSetMerged()) {
-    NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&stream_, cudaStreamNonBlocking));
+SolveGroup::SolveGroup(int lanes) {
+    for (int i = 0; i < std::max(lanes, 1); ++i) {
+        std::unique_ptr<Lane> l(new Lane());
+        NS3D_CUDA_CHECK(cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking));
+        l->set.reset(new KrylovSetMerged());
+        l->mset.reset(new MixedSetMerged());
+        l->set->share = std::max(lanes, 1);  // the lanes' launches run side by side
+        l->mset->share = std::max(lanes, 1);
+        lanes_.push_back(std::move(l));
+    }
 }
 
 SolveGroup::~SolveGroup() {
-    set_.reset();  // their buffers are freed on the group stream
-    mset_.reset();
-    if (stream_) {
-        cudaStreamSynchronize(stream_);
-        cudaStreamDestroy(stream_);
+    for (auto &l : lanes_) {
+        l->set.reset();  // their buffers are freed on the lane's stream
+        l->mset.reset();
+        if (l->stream) {
+            cudaStreamSynchronize(l->stream);
+            cudaStreamDestroy(l->stream);
+        }
     }
 }
 
@@ -60,11 +70,12 @@ SolveGroup::Stats SolveGroup::stats() {
     return stats_;
 }
 
-void SolveGroup::execute(std::vector<Req *> &batch) {
+void SolveGroup::execute(Lane &lane, std::vector<Req *> &batch) {
+    const cudaStream_t st = lane.stream;
     auto fail = [&](int code, const std::string &m) {
         // the members' buffers may still be in use by queued work: drain the
-        // group stream before any member returns with the error
-        cudaStreamSynchronize(stream_);
+        // lane's stream before any member returns with the error
+        cudaStreamSynchronize(st);
         for (Req *q : batch) {
             q->err_code = code;
             q->err = m;
@@ -73,22 +84,22 @@ void SolveGroup::execute(std::vector<Req *> &batch) {
     try {
         std::vector<SolveItem> all;
         for (Req *q : batch) {
-            NS3D_CUDA_CHECK(cudaStreamWaitEvent(stream_, q->ready, 0));
+            NS3D_CUDA_CHECK(cudaStreamWaitEvent(st, q->ready, 0));
             all.insert(all.end(), q->items->begin(), q->items->end());
         }
         std::vector<SolveOutcome> out;
         const int kind = batch.front()->kind;
-        if (kind == 0) set_->run(all, stream_, out);
-        else mset_->run(all, stream_, out, kind - 1);
+        if (kind == 0) lane.set->run(all, st, out);
+        else lane.mset->run(all, st, out, kind - 1);
         size_t off = 0;
         for (Req *q : batch) {
             const size_t n = q->items->size();
             q->out->assign(out.begin() + off, out.begin() + off + n);
-            const KState *src = kind == 0 ? set_->device_state((int)off) : mset_->device_state((int)off);
+            const KState *src = kind == 0 ? lane.set->device_state((int)off) : lane.mset->device_state((int)off);
             if (q->dst && n)
                 NS3D_CUDA_CHECK(
-                    cudaMemcpyAsync(q->dst, src, n * sizeof(KState), cudaMemcpyDeviceToDevice, stream_));
-            NS3D_CUDA_CHECK(cudaEventRecord(q->fin, stream_));
+                    cudaMemcpyAsync(q->dst, src, n * sizeof(KState), cudaMemcpyDeviceToDevice, st));
+            NS3D_CUDA_CHECK(cudaEventRecord(q->fin, st));
             off += n;
         }
     } catch (const ApiError &e) {
@@ -140,21 +151,34 @@ void SolveGroup::submit(Req &r) {
     pending_.push_back(&r);
     cv_.notify_all();
     while (!r.done) {
-        if (leading_ || r.taken) {
+        Lane *lane = nullptr;
+        if (!r.taken)
+            for (auto &l : lanes_)
+                if (!l->busy) {
+                    lane = l.get();
+                    break;
+                }
+        if (!lane) {  // taken by a leader, or every lane busy
             cv_.wait(lk);
             continue;
         }
-        // lead one merged launch
-        leading_ = true;
+        // lead one merged solve on this lane: wait (up to the window) for a
+        // cohort, then take the oldest queued set and the later ones of its
+        // kind, in arrival order, while they fit the cohort and the set
+        lane->busy = true;
+        const int cohort = std::max(1, (members_ + lanes() - 1) / lanes());
         const auto deadline = std::chrono::steady_clock::now() + std::chrono::duration<double>(window_s);
-        cv_.wait_until(lk, deadline, [&] { return (int)pending_.size() >= members_; });
-        // the oldest queued set and the later ones of its kind, in arrival
-        // order, while they fit
+        cv_.wait_until(lk, deadline, [&] { return (int)pending_.size() >= cohort; });
+        if (pending_.empty()) {  // another lane's leader took every queued set (this one's too)
+            lane->busy = false;
+            cv_.notify_all();
+            continue;
+        }
         std::vector<Req *> batch;
         batch.reserve(pending_.size());
         int systems = 0;
         const int kind = pending_.front()->kind;
-        for (auto it = pending_.begin(); it != pending_.end();) {
+        for (auto it = pending_.begin(); it != pending_.end() && (int)batch.size() < cohort;) {
             Req *q = *it;
             const int n = (int)q->items->size();
             if (q->kind != kind) {
@@ -173,10 +197,10 @@ void SolveGroup::submit(Req &r) {
         stats_.max_systems = std::max(stats_.max_systems, systems);
         stats_.max_requests = std::max(stats_.max_requests, (int)batch.size());
         lk.unlock();
-        execute(batch);
+        execute(*lane, batch);
         lk.lock();
         for (Req *q : batch) q->done = true;
-        leading_ = false;
+        lane->busy = false;
         cv_.notify_all();
     }
     lk.unlock();
@@ -190,14 +214,15 @@ using namespace ns3d;
 
 struct ns3d_group {
     SolveGroup g;
+    explicit ns3d_group(int lanes) : g(lanes) {}
 };
 
 extern "C" {
 
-NS3D_API int ns3d_group_create(ns3d_group **out) {
-    if (!out) return report_error(NS3D_ERR_ARG, "NULL argument");
+NS3D_API int ns3d_group_create(int32_t lanes, ns3d_group **out) {
+    if (!out || lanes < 1 || lanes > 16) return report_error(NS3D_ERR_ARG, "bad argument");
     try {
-        *out = new ns3d_group();
+        *out = new ns3d_group(lanes);
         return NS3D_OK;
     } catch (const CudaError &e) {
         return report_error(NS3D_ERR_CUDA, e.what());

@@ -85,9 +85,10 @@ void launch_face_average(const Grid &g, const double *u, const double *v, const 
 template <int CAP>
 void launch_krylov_init(const KSetArgT<CAP> &set, cudaStream_t st);
 // iterations until every system is done, one needs a restart, or max_iters
+// (a merged set takes 1/share of the SMs: `share` merged sets run at once)
 template <int CAP>
 cudaError_t launch_krylov_loop(const KSetArgT<CAP> &set, GridBar *bar, LoopProf *prof, int max_iters,
-                               cudaStream_t st);
+                               cudaStream_t st, int share = 1);
 template <int CAP>
 void launch_krylov_restart(const KSetArgT<CAP> &set, cudaStream_t st);
 // blocks of a loop-kernel launch over `units` work units, units_per_chunk

@@ -570,16 +570,18 @@ int loop_grid(int units, int units_per_chunk, int occ) {
     return std::max(1, std::min(std::max(dense, std::min(fair, units)), slots));
 }
 
-// A merged set (the systems of many concurrent solves) spreads over every SM.
+// A merged set (the systems of many concurrent solves) spreads over its
+// share of the SMs: all of them, or 1/share while `share` merged sets run.
 template <int CAP>
-static int krylov_loop_grid(int total_chunks, int occ) {
-    if (CAP > KMAX) return std::max(1, std::min(total_chunks, device_sm_count() * std::max(occ, 1)));
+static int krylov_loop_grid(int total_chunks, int occ, int share) {
+    if (CAP > KMAX)
+        return std::max(1, std::min(total_chunks, device_sm_count() * std::max(occ, 1) / std::max(share, 1)));
     return loop_grid(total_chunks, 1, occ);
 }
 
 template <int CAP>
 cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *prof, int max_iters,
-                               cudaStream_t st) {
+                               cudaStream_t st, int share) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
     static std::atomic<int> loop_occ{0};
     int occ = loop_occ.load();
@@ -589,7 +591,7 @@ cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *p
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         loop_occ = occ;
     }
-    const int grid = krylov_loop_grid<CAP>(A.total_chunks, occ);
+    const int grid = krylov_loop_grid<CAP>(A.total_chunks, occ, share);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     KSetArgT<CAP> a = A;
@@ -607,9 +609,9 @@ void launch_krylov_restart(const KSetArgT<CAP> &A, cudaStream_t st) {
 
 template void launch_krylov_init<KMAX>(const KSetArg &, cudaStream_t);
 template void launch_krylov_init<KMAX_MERGED>(const KSetArgMerged &, cudaStream_t);
-template cudaError_t launch_krylov_loop<KMAX>(const KSetArg &, GridBar *, LoopProf *, int, cudaStream_t);
+template cudaError_t launch_krylov_loop<KMAX>(const KSetArg &, GridBar *, LoopProf *, int, cudaStream_t, int);
 template cudaError_t launch_krylov_loop<KMAX_MERGED>(const KSetArgMerged &, GridBar *, LoopProf *, int,
-                                                     cudaStream_t);
+                                                     cudaStream_t, int);
 template void launch_krylov_restart<KMAX>(const KSetArg &, cudaStream_t);
 template void launch_krylov_restart<KMAX_MERGED>(const KSetArgMerged &, cudaStream_t);
 

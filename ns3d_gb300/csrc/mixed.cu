@@ -974,7 +974,8 @@ constexpr long kFusedRows = 1L << 19;
 bool m32_fused(long rows, bool mg) { return rows <= kFusedRows && !mg; }
 
 template <int CAP>
-cudaError_t launch_m32_loop(const MSetArgT<CAP> &A, GridBar *bar, int max_iters, cudaStream_t st, int variant) {
+cudaError_t launch_m32_loop(const MSetArgT<CAP> &A, GridBar *bar, int max_iters, cudaStream_t st, int variant,
+                            int share) {
     if (A.total_chunks <= 0 || max_iters <= 0) return cudaSuccess;
     long rows = 0;
     bool mg = false;
@@ -992,9 +993,10 @@ cudaError_t launch_m32_loop(const MSetArgT<CAP> &A, GridBar *bar, int max_iters,
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         occ_cache[fused] = occ;
     }
-    // a merged set (many solves' systems) spreads over every SM
-    const int grid = CAP > KMAX ? std::max(1, std::min(A.total_chunks * MSUB, device_sm_count() * occ))
-                                : loop_grid(A.total_chunks * MSUB, MSUB, occ);
+    // a merged set (many solves' systems) spreads over its share of the SMs
+    const int grid = CAP > KMAX
+                         ? std::max(1, std::min(A.total_chunks * MSUB, device_sm_count() * occ / std::max(share, 1)))
+                         : loop_grid(A.total_chunks * MSUB, MSUB, occ);
     cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
     if (e != cudaSuccess) return e;
     MSetArgT<CAP> a = A;
@@ -1015,8 +1017,8 @@ template void launch_dc_resid<KMAX>(const MSetArg &, int, cudaStream_t);
 template void launch_dc_resid<KMAX_MERGED_M>(const MSetArgMerged &, int, cudaStream_t);
 template void launch_m32_init<KMAX>(const MSetArg &, cudaStream_t);
 template void launch_m32_init<KMAX_MERGED_M>(const MSetArgMerged &, cudaStream_t);
-template cudaError_t launch_m32_loop<KMAX>(const MSetArg &, GridBar *, int, cudaStream_t, int);
-template cudaError_t launch_m32_loop<KMAX_MERGED_M>(const MSetArgMerged &, GridBar *, int, cudaStream_t, int);
+template cudaError_t launch_m32_loop<KMAX>(const MSetArg &, GridBar *, int, cudaStream_t, int, int);
+template cudaError_t launch_m32_loop<KMAX_MERGED_M>(const MSetArgMerged &, GridBar *, int, cudaStream_t, int, int);
 template void launch_dc_update<KMAX>(const MSetArg &, cudaStream_t);
 template void launch_dc_update<KMAX_MERGED_M>(const MSetArgMerged &, cudaStream_t);
 

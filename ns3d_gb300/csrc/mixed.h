@@ -87,10 +87,11 @@ void launch_m32_init(const MSetArgT<CAP> &set, cudaStream_t st);
 // five-phase loop.  A merged set runs the variant its members chose alone.
 bool m32_fused(long rows, bool mg);
 // FP32 inner iterations until every inner solve of the round is done
-// (variant: -1 from the set's own rows, 0 five-phase, 1 fused)
+// (variant: -1 from the set's own rows, 0 five-phase, 1 fused; a merged set
+// takes 1/share of the SMs)
 template <int CAP>
 cudaError_t launch_m32_loop(const MSetArgT<CAP> &set, GridBar *bar, int max_iters, cudaStream_t st,
-                            int variant = -1);
+                            int variant = -1, int share = 1);
 // theta = <r, A d> / <A d, A d> for the FP32 correction d (FP64 SpMV), then
 // x += theta d
 template <int CAP>

@@ -4,6 +4,7 @@
 
 #include "mixed.h"
 #include "runtime.h"
+#include "tuner.h"
 
 namespace ns3d {
 
@@ -225,6 +226,19 @@ void MixedSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st, s
     // maxit + 2 rounds bound the loop; each round's inner loop is bounded by
     // the remaining iteration budget.
     long rounds = 0;
+    // merged sets: the grid of each FP32 loop launch comes from the
+    // autotuner, told the launch's time per inner row-iteration
+    const bool tune = CAP > KMAX;
+    int cand = 0, kind = 0;
+    if (tune) {
+        bool mg = false;
+        for (int i = 0; i < ns; ++i) mg = mg || set_.sys[i].mg.nlev > 0;
+        kind = mg ? 3 : (variant == 1 ? 2 : 1);
+        if (!ev_[0])
+            for (cudaEvent_t &e : ev_) NS3D_CUDA_CHECK(cudaEventCreate(&e));
+    }
+    const uint64_t tkey = tuner_key(kind, (long)total_chunks_ * MSUB, share);
+    std::vector<int> iters_before(ns, 0);
     // One round = FP32 init, the FP32 loop kernel (it ends when every inner
     // solve of the round is done: each is capped by the remaining iteration
     // budget), the FP64 update and residual; the host reads the outer state
@@ -235,12 +249,25 @@ void MixedSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st, s
         NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
         if (rounds > 0 && h_err_.p[0])
             throw ApiError(NS3D_ERR_TIMEOUT, "FP32 BiCGSTAB loop kernel: a grid barrier timed out");
+        if (tune && rounds > 0) {  // inner iterations of the round, from the FP64 states
+            double rows = 0;
+            for (int i = 0; i < ns; ++i) rows += (double)set_.sys[i].n * (h_dc_.p[i].total_iter - iters_before[i]);
+            float ms = 0;
+            NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+            grid_tuner().report(tkey, cand, ms, rows);
+        }
+        for (int i = 0; i < ns; ++i) iters_before[i] = h_dc_.p[i].total_iter;
         bool all_done = true;
         for (int i = 0; i < ns; ++i) all_done = all_done && h_dc_.p[i].done;
         if (all_done) break;
         if (++rounds > maxit + 2L) throw ApiError(NS3D_ERR_TIMEOUT, "defect correction exceeded its round bound");
         launch_m32_init(set_, st);
-        NS3D_CUDA_CHECK(launch_m32_loop(set_, bar_.p, maxit + 64, st, variant));
+        if (tune) {
+            cand = grid_tuner().choose(tkey);
+            NS3D_CUDA_CHECK(cudaEventRecord(ev_[0], st));
+        }
+        NS3D_CUDA_CHECK(launch_m32_loop(set_, bar_.p, maxit + 64, st, variant, share << cand));
+        if (tune) NS3D_CUDA_CHECK(cudaEventRecord(ev_[1], st));
         launch_dc_update(set_, st);
         launch_dc_resid(set_, 0, st);
     }
@@ -262,6 +289,12 @@ void MixedSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st, s
         h_out_.p[i] = k;
     }
     NS3D_CUDA_CHECK(cudaMemcpyAsync(out_st_.p, h_out_.p, ns * sizeof(KState), cudaMemcpyHostToDevice, st));
+}
+
+template <int CAP>
+MixedSetT<CAP>::~MixedSetT() {
+    for (cudaEvent_t e : ev_)
+        if (e) cudaEventDestroy(e);
 }
 
 template class MixedSetT<KMAX>;

@@ -189,6 +189,7 @@ class KrylovSetT {
     };
     bool profiling = false;
     Profile prof;
+    int share = 1;  // a merged set's loop launches take 1/share of the SMs
     ~KrylovSetT();
 
   private:
@@ -240,10 +241,12 @@ class MixedSetT {
     bool use_mg = false;                          // multilevel preconditioner for single-system sets
     double inner_rel_tol = NS3D_MIXED_INNER_TOL;  // floor of the per-round FP32 reduction target
     int inner_cap = NS3D_MIXED_INNER_CAP;         // FP32 iterations per round at most
-    ~MixedSetT() = default;
+    int share = 1;                                // a merged set's loop launches take 1/share of the SMs
+    ~MixedSetT();
 
   private:
     void configure(const std::vector<SolveItem> &items, cudaStream_t st);
+    cudaEvent_t ev_[2] = {nullptr, nullptr};  // around the FP32 loop launch (merged sets: autotuner timing)
     DBuf<KState> st_, out_st_;
     DBuf<DCState> dc_;
     HBuf<KState> h_st_, h_out_;
@@ -260,17 +263,20 @@ using MixedSetMerged = MixedSetT<KMAX_MERGED_M>;
 // The BiCGSTAB work of many concurrent solver instances merged into shared
 // persistent kernels: each member's solve sets (its momentum components,
 // its pressure system; FP64, or FP32 inside FP64 defect correction) are
-// queued here, and one member at a time (the leader) gathers the queued sets
-// of one kind -- FP64, or mixed precision with one FP32 loop variant -- up to
+// queued here, and a member (the leader of a lane) gathers queued sets of
+// one kind -- FP64, or mixed precision with one FP32 loop variant -- up to
 // KMAX_MERGED (FP64) or KMAX_MERGED_M (mixed) systems, and solves them
-// together on the group's own stream: every launch covers the ragged list of
-// all their 1024-row chunks.  The leader waits for the other members up to a
-// short window (the members run their outer iterations in near lockstep),
-// so the launches stay full.  Each system keeps its own scalars, reduction
-// order and preconditioner, so a solve gives the same bits alone and merged.
+// together on the lane's stream: every launch covers the ragged list of all
+// their 1024-row chunks.  The members are split into cohorts, one per lane
+// (at most ceil(members / lanes) sets per merged solve); a leader waits for
+// a full cohort up to a short window (members run their outer iterations in
+// near lockstep), so launches stay full, while the lanes run side by side:
+// one cohort's solves overlap another's assembly and host work.  Each
+// system keeps its own scalars, reduction order and preconditioner, so a
+// solve gives the same bits alone and merged.
 class SolveGroup {
   public:
-    SolveGroup();
+    explicit SolveGroup(int lanes = 1);
     ~SolveGroup();
     // a solve of a member starts / ends (the leader waits for members only)
     void join();
@@ -293,19 +299,24 @@ class SolveGroup {
     Stats stats();
     double window_s = 2e-3;  // longest wait of a leader for the other members
 
+    int lanes() const { return (int)lanes_.size(); }
+
   private:
     struct Req;
+    struct Lane {  // a stream and the merged sets solved on it
+        cudaStream_t stream = nullptr;
+        std::unique_ptr<KrylovSetMerged> set;
+        std::unique_ptr<MixedSetMerged> mset;
+        bool busy = false;
+    };
     void submit(Req &r);
-    void execute(std::vector<Req *> &batch);
+    void execute(Lane &lane, std::vector<Req *> &batch);
     std::mutex mu_;
     std::condition_variable cv_;
     std::deque<Req *> pending_;
     int members_ = 0;
-    bool leading_ = false;
     Stats stats_;
-    cudaStream_t stream_ = nullptr;
-    std::unique_ptr<KrylovSetMerged> set_;
-    std::unique_ptr<MixedSetMerged> mset_;
+    std::vector<std::unique_ptr<Lane>> lanes_;
 };
 // the solve group behind a C-ABI group handle (NULL for NULL)
 SolveGroup *group_of(ns3d_group *g);

@@ -312,17 +312,17 @@ NS3D_API int ns3d_server_stop(ns3d_server *s) {
     return NS3D_OK;
 }
 
-NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t enable) {
-    if (!s) return NS3D_ERR_ARG;
+NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t lanes) {
+    if (!s || lanes < 0) return NS3D_ERR_ARG;
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->any) return NS3D_ERR_STATE;  // before the first request only
-    if (enable && !s->group) {
-        cudaSetDevice(s->device);
-        const int rc = ns3d_group_create(&s->group);
-        if (rc != NS3D_OK) return rc;
-    } else if (!enable && s->group) {
+    if (s->group) {
         ns3d_group_destroy(s->group);
         s->group = nullptr;
+    }
+    if (lanes > 0) {
+        cudaSetDevice(s->device);
+        return ns3d_group_create(lanes, &s->group);
     }
     return NS3D_OK;
 }
@@ -334,13 +334,13 @@ NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out) {
 }
 
 static int batch_solve(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims, int32_t njobs,
-                       int32_t max_concurrent, int32_t merge, ns3d_result *results, int32_t *status,
+                       int32_t max_concurrent, int32_t lanes, ns3d_result *results, int32_t *status,
                        ns3d_group_stats *gstats) {
     if (!params || !raws || !dims || !results || njobs < 0 || max_concurrent <= 0) return NS3D_ERR_ARG;
     ns3d_server *s = nullptr;
     int rc = ns3d_server_start(max_concurrent, 0, &s);
     if (rc != NS3D_OK) return rc;
-    if (merge && (rc = ns3d_server_set_merging(s, 1)) != NS3D_OK) {
+    if (lanes > 0 && (rc = ns3d_server_set_merging(s, lanes)) != NS3D_OK) {
         ns3d_server_stop(s);
         return rc;
     }
@@ -370,9 +370,10 @@ NS3D_API int ns3d_batch_solve(const ns3d_params *params, const uint8_t *const *r
 }
 
 NS3D_API int ns3d_batch_solve_merged(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
-                                     int32_t njobs, int32_t max_concurrent, ns3d_result *results, int32_t *status,
-                                     ns3d_group_stats *stats) {
-    return batch_solve(params, raws, dims, njobs, max_concurrent, 1, results, status, stats);
+                                     int32_t njobs, int32_t max_concurrent, int32_t lanes, ns3d_result *results,
+                                     int32_t *status, ns3d_group_stats *stats) {
+    if (lanes < 1) return NS3D_ERR_ARG;
+    return batch_solve(params, raws, dims, njobs, max_concurrent, lanes, results, status, stats);
 }
 
 }  // extern "C"

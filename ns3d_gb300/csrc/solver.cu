@@ -22,6 +22,7 @@
 
 #include "hostio.h"
 #include "runtime.h"
+#include "tuner.h"
 
 namespace ns3d {
 
@@ -157,6 +158,11 @@ void KrylovSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st,
     long issued = 0;
     int loops = 0;
     std::vector<int> work_before(ns, 0);
+    // merged sets: the grid of each loop launch comes from the autotuner,
+    // which is told the launch's time per row-iteration
+    const bool tune = CAP > KMAX;
+    const uint64_t tkey = tuner_key(0, total_chunks_, share);
+    int cand = 0;
     while (true) {
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_err_.p, &bar_.p->err, sizeof(int), cudaMemcpyDeviceToHost, st));
@@ -175,6 +181,11 @@ void KrylovSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st,
             }
             work_before[i] = k.work;
         }
+        if (tune && loops > 0) {
+            float ms = 0;
+            NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+            grid_tuner().report(tkey, cand, ms, (double)rows);
+        }
         if (profiling && loops > 0) {
             float ms = 0;
             NS3D_CUDA_CHECK(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
@@ -192,9 +203,11 @@ void KrylovSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st,
             launch_krylov_restart(set_, st);
             launches_ += 1;
         }
-        if (profiling) NS3D_CUDA_CHECK(cudaEventRecord(ev_[0], st));
-        NS3D_CUDA_CHECK(launch_krylov_loop(set_, bar_.p, profiling ? prof_.p : nullptr, (int)(cap - issued), st));
-        if (profiling) NS3D_CUDA_CHECK(cudaEventRecord(ev_[1], st));
+        if (tune) cand = grid_tuner().choose(tkey);
+        if (profiling || tune) NS3D_CUDA_CHECK(cudaEventRecord(ev_[0], st));
+        NS3D_CUDA_CHECK(launch_krylov_loop(set_, bar_.p, profiling ? prof_.p : nullptr, (int)(cap - issued), st,
+                                           share << cand));
+        if (profiling || tune) NS3D_CUDA_CHECK(cudaEventRecord(ev_[1], st));
         launches_ += 1;
         loops += 1;
     }

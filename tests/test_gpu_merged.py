@@ -37,12 +37,12 @@ def _alone(lib, reqs):
     return out
 
 
-def _group_solve_and_compare(lib, reqs):
+def _group_solve_and_compare(lib, reqs, lanes=1):
     """Solves every request alone, then all of them at once on their own
     threads with their solvers attached to one group; asserts bit-identical
     results and returns the group's statistics."""
     alone = _alone(lib, reqs)
-    group = capi.Group(lib)
+    group = capi.Group(lib, lanes)
     solvers = [capi.Solver(lib, p, synth.to_raw(img), img.shape) for p, img in reqs]
     for s in solvers:
         group.attach(s)
@@ -72,11 +72,17 @@ def _group_solve_and_compare(lib, reqs):
     return st
 
 
-def test_group_solves_equal_alone(gpulib):
-    st = _group_solve_and_compare(gpulib, _requests(gpulib))
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_group_solves_equal_alone(gpulib, lanes):
+    st = _group_solve_and_compare(gpulib, _requests(gpulib), lanes)
     # the sets were really merged: some launches served several solves
     assert st.launches > 0 and st.max_requests >= 2
     assert st.systems > st.launches
+    if lanes == 2:  # cohorts of ceil(6 / 2) solves
+        assert st.max_requests <= 3
+    # the merged launches were timed for the grid autotuner (which may have
+    # run them on different grids: the results above are bit-identical anyway)
+    assert "kind=0" in capi.autotune_table(gpulib)
 
 
 def test_group_detach_solves_alone(gpulib):
@@ -98,13 +104,13 @@ def test_merged_batch_and_server_match_single_solves(gpulib):
     reqs = _requests(gpulib)[:4]
     alone = _alone(gpulib, reqs)
     res, status, g, rc = capi.batch_solve(gpulib, [p for p, _ in reqs], [synth.to_raw(img) for _, img in reqs],
-                                          [img.shape for _, img in reqs], 4, merged=True)
+                                          [img.shape for _, img in reqs], 4, merged=1)
     assert rc == 0 and not status.any()
     for r, (k, its, _, _, _, _) in zip(res, alone):
         assert r.K == k and r.iterations == its
     assert g.launches > 0 and g.max_requests >= 2
 
-    srv = capi.Server(gpulib, max_active=4, merge=True)
+    srv = capi.Server(gpulib, max_active=4, merge=2)
     tickets = [srv.submit(p, synth.to_raw(img), img.shape, keep_fields=True) for p, img in reqs]
     for t, (k, its, _, _, fields, sizes) in zip(tickets, alone):
         r, lat = srv.wait(t)
@@ -126,5 +132,5 @@ def test_mixed_precision_group_solves_equal_alone(gpulib, precision):
         img, _ = synth.rsa_spheres(shape, r_, phi, seed=90 + k)
         reqs.append((params(gpulib, method=method, direction=direction, maxitSIMPLE=60, simpletol=1e-5,
                             precision=precision), img))
-    st = _group_solve_and_compare(gpulib, reqs)
+    st = _group_solve_and_compare(gpulib, reqs, lanes=2)
     assert st.launches > 0 and st.max_requests >= 2

@@ -46,7 +46,8 @@ def test_oracle_exports_the_solver_symbols(oracle):
                  "ns3d_server_get_stats", "ns3d_server_stop", "ns3d_generate_image",
                  "ns3d_server_cancel_queued", "ns3d_solve_sweep", "ns3d_group_create", "ns3d_set_group",
                  "ns3d_group_get_stats", "ns3d_group_destroy", "ns3d_server_set_merging",
-                 "ns3d_server_group_stats", "ns3d_batch_solve_merged"}
+                 "ns3d_server_group_stats", "ns3d_batch_solve_merged", "ns3d_autotune_enable",
+                 "ns3d_autotune_table"}
     for s in declared_symbols():
         if s not in host_only:
             assert hasattr(oracle, s), s
@@ -183,3 +184,14 @@ def test_golden_fields_decode(gpulib):
     assert p.shape == (128, 128, 128)
     u = ns.read_vti_f64(ref.replace("P-1", "Vx-1"))
     assert u.shape == (129, 128, 128)
+
+
+def test_autotune_switch_and_empty_table(gpulib):
+    """The merged-set autotuner's host interface: modes 0-2, the table of
+    classes (empty before any merged launch), bad arguments rejected."""
+    lib = capi._declare_server(gpulib)
+    assert lib.ns3d_autotune_enable(3) == capi.ERR_ARG
+    assert lib.ns3d_autotune_enable(2) == 0  # forget, stay on
+    assert capi.autotune_table(gpulib) == ""
+    assert lib.ns3d_autotune_table(None, 10) == capi.ERR_ARG
+    assert lib.ns3d_autotune_enable(0) == 0 and lib.ns3d_autotune_enable(1) == 0
