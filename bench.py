@@ -364,8 +364,9 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
 
 # Merged sample (opt-in, --merged): the batch mix above (SIMPLEC, flow x)
 # solved in plain FP64 one image at a time, then as batches of concurrent
-# solves on their own streams (ns3d_batch_solve) and with their BiCGSTAB sets
-# merged into shared persistent launches (ns3d_batch_solve_merged), in plain
+# solves on their own streams (ns3d_batch_solve), with their BiCGSTAB sets
+# merged into shared persistent launches (ns3d_batch_solve_merged), and all
+# driven in lockstep by one host thread (ns3d_batch_solve_lockstep), in plain
 # FP64 and in the serving precision.  The FP64 legs follow the same
 # trajectory bit for bit (fixed-order reductions), so max_outer may cap the
 # outer iterations of every leg alike.
@@ -411,10 +412,16 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
         for lanes in MERGED_LANES:
             legs_spec.append(("batch_%s_merged_%d_lane%s" % (label, lanes, "s" if lanes > 1 else ""), lanes,
                               precision))
+        legs_spec.append(("batch_%s_lockstep" % label, -1, precision))
     for name, merged, precision in legs_spec:
         t = time.perf_counter()
-        res, status, g, rc = capi.batch_solve(lib, [prm(r, precision) for r in imgs], [r["raw"] for r in imgs],
-                                              [r["shape"] for r in imgs], max_concurrent, merged=merged)
+        if merged >= 0:
+            res, status, g, rc = capi.batch_solve(lib, [prm(r, precision) for r in imgs], [r["raw"] for r in imgs],
+                                                  [r["shape"] for r in imgs], max_concurrent, merged=merged)
+        else:  # every image resident, all driven in lockstep by one thread
+            res, status, rc = capi.batch_solve_lockstep(lib, [prm(r, precision) for r in imgs],
+                                                        [r["raw"] for r in imgs], [r["shape"] for r in imgs])
+            g = None
         dt = time.perf_counter() - t
         leg = {"solves_per_s": n_images / dt, "seconds": dt, "status": int(rc),
                "speedup_vs_one_at_a_time": t1 / dt, "max_concurrent": max_concurrent}

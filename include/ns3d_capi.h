@@ -371,6 +371,23 @@ NS3D_API int ns3d_group_destroy(ns3d_group *g);
 NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t lanes);
 NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out);
 /*
+ * Lockstep solves (no counterpart in the reference, which solves one image
+ * per process): the SIMPLEC solves (SIMPLECSOLVER::Solve, src/SIMPLEC.cxx:
+ * 73-232) of n opened handles driven together by the calling thread.  Every
+ * image takes exactly its own steps -- result, fields and logs are
+ * bit-identical to ns3d_solve of that handle -- but each step runs for all
+ * images at once: their kernels on one stream, each BiCGSTAB step as merged
+ * sets (one persistent launch per round over the ragged chunk lists of all
+ * images, by each image's precision), one host wait per read-back for all.
+ * Every handle must use method SIMPLEC; status[i] (may be NULL) receives
+ * each outcome.  The batch form opens, solves and closes n images (all of
+ * them resident at once).
+ */
+NS3D_API int ns3d_solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status);
+NS3D_API int ns3d_batch_solve_lockstep(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                                       int32_t n, ns3d_result *results, int32_t *status);
+
+/*
  * Autotuner of merged solve sets (no counterpart in the reference).  The
  * persistent loop kernel of a merged set may run on any number of blocks
  * without changing a bit of the results (fixed-order reductions); the

@@ -21,7 +21,7 @@ EXE = os.path.join(LIBDIR, "NS3D")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 CU_FILES = ["geometry.cu", "physics.cu", "krylov.cu", "solver.cu", "noalloc.cu", "mixed.cu", "mixed_host.cu", "imagegen.cu",
-            "group.cu"]
+            "group.cu", "lockstep.cu"]
 CPP_FILES = ["hostio.cpp", "capi_host.cpp", "serving.cpp", "tuner.cpp"]
 
 

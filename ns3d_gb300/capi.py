@@ -296,6 +296,8 @@ def _declare_server(lib):
         "ns3d_set_group": (C.c_int, [C.c_void_p, C.c_void_p]),
         "ns3d_group_get_stats": (C.c_int, [C.c_void_p, _P(GroupStats)]),
         "ns3d_group_destroy": (C.c_int, [C.c_void_p]),
+        "ns3d_solve_lockstep": (C.c_int, [_P(C.c_void_p), C.c_int32, _i32]),
+        "ns3d_batch_solve_lockstep": (C.c_int, [_P(Params), _P(_P(C.c_uint8)), _i32, C.c_int32, _P(Result), _i32]),
         "ns3d_autotune_enable": (C.c_int, [C.c_int32]),
         "ns3d_autotune_table": (C.c_int, [C.c_char_p, C.c_int32]),
     }
@@ -459,3 +461,28 @@ def autotune_table(lib):
     buf = C.create_string_buffer(1 << 16)
     lib.ns3d_autotune_table(buf, len(buf))
     return buf.value.decode()
+
+
+def solve_lockstep(lib, solvers):
+    """ns3d_solve_lockstep: the SIMPLEC solves of `solvers` driven together by
+    this thread.  Returns (return code, per-solver statuses)."""
+    lib = _declare_server(lib)
+    n = len(solvers)
+    hs = (C.c_void_p * n)(*[s.h.value for s in solvers])
+    st = np.zeros(n, np.int32)
+    rc = lib.ns3d_solve_lockstep(hs, n, _ptr(st, C.c_int32))
+    return rc, st
+
+
+def batch_solve_lockstep(lib, params_list, images_xfastest, dims_list):
+    """ns3d_batch_solve_lockstep over host images: (results, statuses, return code)."""
+    lib = _declare_server(lib)
+    n = len(params_list)
+    raws = [np.ascontiguousarray(r, dtype=np.uint8).reshape(-1) for r in images_xfastest]
+    ptrs = (_P(C.c_uint8) * n)(*[_ptr(r, C.c_uint8) for r in raws])
+    dims = np.ascontiguousarray(np.array(dims_list, np.int32).reshape(-1))
+    ps = (Params * n)(*params_list)
+    res = (Result * n)()
+    st = np.zeros(n, np.int32)
+    rc = lib.ns3d_batch_solve_lockstep(ps, ptrs, _ptr(dims, C.c_int32), n, res, _ptr(st, C.c_int32))
+    return list(res), st, rc

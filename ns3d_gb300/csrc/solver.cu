@@ -20,6 +20,7 @@
 #include <string>
 #include <vector>
 
+#include "handle.h"
 #include "hostio.h"
 #include "runtime.h"
 #include "tuner.h"
@@ -249,128 +250,9 @@ static int set_error(int code, const std::string &m) {
 
 int report_error(int code, const std::string &m) { return set_error(code, m); }
 
-struct Scalars {
-    double Q = 0, v_moy = 0, K = 0, normdiv = 0, reldiv = 0, velocityNorm = 0, maxdiv = 0, MaxDeltaV = 0;
-};
-
 }  // namespace ns3d
 
 using namespace ns3d;
-
-struct ns3d_handle {
-    ns3d_params prm;
-    int rnx = 0, rny = 0, rnz = 0;  // raw image
-    int nx = 0, ny = 0, nz = 0;     // solver frame
-    int np = 0, nu = 0, nv = 0, nw = 0;
-    OwnedStream owned_stream;  // destroyed after every buffer freed on it
-    cudaStream_t stream = nullptr;
-
-    DBuf<uint8_t> img;
-    DBuf<int> pmap, umap, vmap, wmap;
-    DevSys U, V, W, P;
-    // fields and work vectors (npad of their system)
-    DBuf<double> p, u, v, w, pc, ptemp, utemp, vtemp, wtemp, uh, vh, wh, ut, vt, wt;
-    DBuf<double> diag_part;
-    DBuf<DiagOut> diag;
-    HBuf<DiagOut> h_diag;
-    KrylovSet kmom, kp;
-    MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
-    SolveGroup *group = nullptr;  // sets merged with other solves' (ns3d_set_group)
-    bool mixed() const { return prm.precision != NS3D_FP64; }
-    // an FP64 set: alone, or merged with the sets of the group's other solves
-    void run_fp64(KrylovSet &own, const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
-        if (!group) {
-            own.run(items, stream, out);
-            return;
-        }
-        own.prepare(items, stream);  // the merged run leaves the final states here
-        group->run(items, stream, own.state_buffer(), out);
-    }
-    // a mixed-precision set: alone, or merged (with the preconditioner and
-    // FP32 loop variant its own set chooses)
-    void run_mixed(MixedSet &own, std::vector<SolveItem> items, std::vector<SolveOutcome> &out) {
-        if (!group) {
-            own.run(items, stream, out);
-            return;
-        }
-        own.prepare(items, stream);  // FP32 copies, hierarchy, outcome states
-        for (size_t i = 0; i < items.size(); ++i) items[i].mg = own.uses_mg((int)i);
-        group->run_mixed(items, stream, own.out_state_buffer(), out, own.variant());
-    }
-    void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
-        if (mixed()) run_mixed(mp, items, out);
-        else run_fp64(kp, items, out);
-    }
-
-    // physical constants and relaxation state (NavierStokesBase members)
-    double dx, dy, dz, mu, rho, p0, p1, gradp, alpha0, beta0, alpha, beta;
-    double p_inlet = 0, p_outlet = 0, schemefactor, min_alpha, min_beta, relax, speedup, maxconvdelta;
-    double RMR = 0, old_RMR = 0, deltaRMR, pcmax = 0, pcmin = 0, pcnorm = 0;
-    int border;
-    std::list<double> avgRMR;
-    SolveOutcome su, sv, sw, sp;
-
-    ns3d_result res;
-    std::string outdir, stem;
-    bool write_fields = false, have_out = false;
-    TextLog info, resl;
-
-    Grid grid() const {
-        Grid g;
-        g.nx = nx; g.ny = ny; g.nz = nz;
-        g.pmap = pmap.p; g.umap = umap.p; g.vmap = vmap.p; g.wmap = wmap.p;
-        return g;
-    }
-    Phys phys() const {
-        Phys ph;
-        ph.dx = dx; ph.dy = dy; ph.dz = dz; ph.mu = mu; ph.rho = rho; ph.alpha = alpha; ph.beta = beta;
-        ph.p0 = p0; ph.p1 = p1; ph.schemefactor = schemefactor;
-        ph.idx = 1 / dx; ph.idy = 1 / dy; ph.idz = 1 / dz;
-        ph.idx2 = 1 / (dx * dx); ph.idy2 = 1 / (dy * dy); ph.idz2 = 1 / (dz * dz);
-        return ph;
-    }
-
-    // ---------------------------------------------------------------------
-    void build(const uint8_t *raw, int rx, int ry, int rz);
-    void default_fields();
-    void set_pressure_drop(double p0_in, double gradp_in);
-    void assemble_all_momentum();
-    void momentum_rhs();
-    void compute_velocity_field(bool limit, double dvmax);
-    void log_solve(const char *comp, const SolveOutcome &o);
-    void log_pressure_status(const SolveOutcome &o);
-    void compute_pressure_correction();
-    void compute_pressure_field();
-    void correct_pressure_field();
-    void permeability(Scalars &s);
-    void divergence(Scalars &s);
-    void diagnostics(Scalars &s);
-    void relax_control(bool beta_cst);
-    bool check_convergence(double res_, double tol) const;
-    void pressure_step(bool relax_p, const double *uc, const double *vc, const double *wc, const double *uold,
-                       const double *vold, const double *wold, double *ux, double *vx, double *wx);
-    void hats(const double *uc, const double *vc, const double *wc, const double *uold, const double *vold,
-              const double *wold);
-    void res_row(int it, const Scalars &s);
-    void fields_to_image(const std::string &file);
-    void save_snapshot(int it, int &savecounter);
-    void header(const char *name, const char *maxname);
-    void finish(const char *name, int it, const Scalars &s, std::chrono::steady_clock::time_point t0, time_t start);
-    void initial_velocity(Scalars &s);
-    void run_simplec();
-    void run_simpler_family(int method);
-    void old_rmr_update(int it) {
-        if (it > 1) {
-            if (RMR < old_RMR) old_RMR = RMR;
-        } else {
-            old_RMR = RMR;
-        }
-    }
-    void sync() { NS3D_CUDA_CHECK(cudaStreamSynchronize(stream)); }
-    void d2d(double *dst, const double *src, size_t n) {
-        if (n) NS3D_CUDA_CHECK(cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, stream));
-    }
-};
 
 // ---- geometry -----------------------------------------------------------------
 void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
@@ -472,16 +354,31 @@ void ns3d_handle::log_solve(const char *comp, const SolveOutcome &o) {
 // ComputeVelocityField, src/NSBase.cxx:1773-1884: the three components are
 // solved together by one BiCGSTAB loop launch
 void ns3d_handle::compute_velocity_field(bool limit, double dvmax) {
+    const std::vector<SolveItem> items = velocity_begin();
+    std::vector<SolveOutcome> out;
+    if (mixed()) run_mixed(mmom, items, out);
+    else run_fp64(kmom, items, out);
+    velocity_end(out, limit, dvmax);
+}
+
+// the right-hand sides, the previous velocities, and the three systems
+std::vector<SolveItem> ns3d_handle::velocity_begin() {
     momentum_rhs();
     d2d(utemp.p, u.p, U.npad);
     d2d(vtemp.p, v.p, V.npad);
     if (nw > 0) d2d(wtemp.p, w.p, W.npad);
+    return momentum_items();
+}
+
+std::vector<SolveItem> ns3d_handle::momentum_items() {
     std::vector<SolveItem> items = {{&U, u.p, U.rhs.p, prm.vsolvertol, prm.maxitsolver},
                                     {&V, v.p, V.rhs.p, prm.vsolvertol, prm.maxitsolver}};
     if (nw > 0) items.push_back({&W, w.p, W.rhs.p, prm.vsolvertol, prm.maxitsolver});
-    std::vector<SolveOutcome> out;
-    if (mixed()) run_mixed(mmom, items, out);
-    else run_fp64(kmom, items, out);
+    return items;
+}
+
+// revert or clamp each component by its solve's outcome; counts and logs
+void ns3d_handle::velocity_end(const std::vector<SolveOutcome> &out, bool limit, double dvmax) {
     auto state = [&](int i) { return mixed() ? mmom.device_state(i) : kmom.device_state(i); };
     launch_velocity_post(utemp.p, u.p, nu, state(0), limit, dvmax, stream);
     launch_velocity_post(vtemp.p, v.p, nv, state(1), limit, dvmax, stream);
@@ -512,9 +409,22 @@ void ns3d_handle::log_pressure_status(const SolveOutcome &o) {
 
 // ComputePressureCorrection, src/NSBase.cxx:2337-2365
 void ns3d_handle::compute_pressure_correction() {
-    info.s("Solving for pressure correction : ");
+    const std::vector<SolveItem> items = pressure_correction_begin();
     std::vector<SolveOutcome> out;
-    solve_p({{&P, pc.p, P.rhs.p, prm.pcsolvertol, prm.maxitsolver}}, out);
+    solve_p(items, out);
+    pressure_correction_end(out);
+}
+
+std::vector<SolveItem> ns3d_handle::pressure_correction_begin() {
+    info.s("Solving for pressure correction : ");
+    return pressure_correction_items();
+}
+
+std::vector<SolveItem> ns3d_handle::pressure_correction_items() {
+    return {{&P, pc.p, P.rhs.p, prm.pcsolvertol, prm.maxitsolver}};
+}
+
+void ns3d_handle::pressure_correction_end(const std::vector<SolveOutcome> &out) {
     sp = out[0];
     res.krylov_iterations += sp.work;
     res.krylov_rows += (int64_t)sp.work * np;
@@ -544,7 +454,18 @@ void ns3d_handle::compute_pressure_field() {
 
 // CorrectPressureField, src/NSBase.cxx:2367-2380
 void ns3d_handle::correct_pressure_field() {
+    correct_pressure_launch();
+    correct_pressure_read();
+}
+
+void ns3d_handle::correct_pressure_launch() {
     launch_correct_pressure(P.view(), pc.p, p.p, beta, diag_part.p, diag.p, stream);
+}
+
+// Each *_read copies the reduction results to the host and waits for the
+// stream: with many instances on one stream, the first read waits for every
+// instance's launches and the others find them done.
+void ns3d_handle::correct_pressure_read() {
     NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
     sync();
     const DiagOut &d = *h_diag.p;
@@ -558,7 +479,13 @@ void ns3d_handle::correct_pressure_field() {
 // ---- diagnostics ------------------------------------------------------------------
 // ComputePermeability, src/NSBase.cxx:1886-1956
 void ns3d_handle::permeability(Scalars &s) {
-    launch_permeability(grid(), u.p, p.p, border, diag_part.p, diag.p, stream);
+    permeability_launch();
+    permeability_read(s);
+}
+
+void ns3d_handle::permeability_launch() { launch_permeability(grid(), u.p, p.p, border, diag_part.p, diag.p, stream); }
+
+void ns3d_handle::permeability_read(Scalars &s) {
     NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
     sync();
     const DiagOut &d = *h_diag.p;
@@ -585,7 +512,15 @@ void ns3d_handle::permeability(Scalars &s) {
 
 // ComputeDiv, src/NSBase.cxx:1958-2080
 void ns3d_handle::divergence(Scalars &s) {
+    divergence_launch();
+    divergence_read(s);
+}
+
+void ns3d_handle::divergence_launch() {
     launch_divergence(grid(), phys(), P.view(), u.p, v.p, w.p, diag_part.p, diag.p, stream);
+}
+
+void ns3d_handle::divergence_read(Scalars &s) {
     NS3D_CUDA_CHECK(cudaMemcpyAsync(h_diag.p, diag.p, sizeof(DiagOut), cudaMemcpyDeviceToHost, stream));
     sync();
     const DiagOut &d = *h_diag.p;
@@ -598,6 +533,11 @@ void ns3d_handle::divergence(Scalars &s) {
 void ns3d_handle::diagnostics(Scalars &s) {
     permeability(s);
     divergence(s);
+    diagnostics_end(s);
+}
+
+// RMR, relative divergence and the K line from the two reductions
+void ns3d_handle::diagnostics_end(Scalars &s) {
     RMR = s.MaxDeltaV / std::fabs(s.v_moy);
     s.reldiv = (nx * dx + ny * dy + nz * dz) * s.maxdiv / (3 * s.v_moy);
     info.s("Permeability K (m²): ").d(s.K).nl();
@@ -1078,17 +1018,22 @@ NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, 
     NS3D_CATCH
 }
 
+// the state a solve starts from: no result, initial relaxation, no history
+void ns3d_handle::begin_solve() {
+    std::memset(&res, 0, sizeof res);
+    su = sv = sw = sp = SolveOutcome();
+    alpha = alpha0;
+    beta = beta0;
+    avgRMR.clear();
+    RMR = old_RMR = 0;
+    kmom.reset_launch_count();
+    kp.reset_launch_count();
+}
+
 NS3D_API int ns3d_solve(ns3d_handle *H) {
     NS3D_TRY
     ns3d_handle &h = *checked(H);
-    std::memset(&h.res, 0, sizeof h.res);
-    h.su = h.sv = h.sw = h.sp = SolveOutcome();
-    h.alpha = h.alpha0;
-    h.beta = h.beta0;
-    h.avgRMR.clear();
-    h.RMR = h.old_RMR = 0;
-    h.kmom.reset_launch_count();
-    h.kp.reset_launch_count();
+    h.begin_solve();
     // while several solves run at once the loop kernels take fewer SMs each
     ActiveSolve active;
     struct Member {  // a merged solve counts as a member of its group while it runs
@@ -1104,6 +1049,56 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
     else h.run_simpler_family(h.prm.method);
     return NS3D_OK;
     NS3D_CATCH
+}
+
+static int solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status) {
+    NS3D_TRY
+    if (n < 0 || (n > 0 && !hs)) throw ApiError(NS3D_ERR_ARG, "ns3d_solve_lockstep: bad arguments");
+    for (int i = 0; i < n; ++i) {
+        const ns3d_handle &h = *checked(hs[i]);
+        if (h.prm.method != NS3D_SIMPLEC) throw ApiError(NS3D_ERR_ARG, "lockstep solves run SIMPLEC only");
+        for (int j = 0; j < i; ++j)
+            if (hs[j] == hs[i]) throw ApiError(NS3D_ERR_ARG, "ns3d_solve_lockstep: a handle appears twice");
+    }
+    if (n == 0) return NS3D_OK;
+    return lockstep_solve(hs, n, status);
+    NS3D_CATCH
+}
+
+NS3D_API int ns3d_solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status) {
+    const int rc = solve_lockstep(hs, n, status);
+    if (rc != NS3D_OK && status)
+        for (int i = 0; i < n; ++i) status[i] = rc;
+    return rc;
+}
+
+NS3D_API int ns3d_batch_solve_lockstep(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
+                                       int32_t n, ns3d_result *results, int32_t *status) {
+    if (!params || !raws || !dims || !results || n < 0) return set_error(NS3D_ERR_ARG, "bad batch arguments");
+    std::vector<ns3d_handle *> hs;
+    std::vector<int> idx;
+    int worst = NS3D_OK;
+    for (int i = 0; i < n; ++i) {
+        std::memset(&results[i], 0, sizeof results[i]);
+        ns3d_handle *h = nullptr;
+        const int rc = ns3d_open(&params[i], raws[i], dims[3 * i], dims[3 * i + 1], dims[3 * i + 2], &h);
+        if (status) status[i] = rc;
+        if (rc != NS3D_OK) {
+            worst = rc;
+            continue;
+        }
+        hs.push_back(h);
+        idx.push_back(i);
+    }
+    std::vector<int32_t> st(hs.size(), NS3D_OK);
+    const int rc = ns3d_solve_lockstep(hs.data(), (int32_t)hs.size(), st.data());
+    if (rc != NS3D_OK) worst = rc;
+    for (size_t k = 0; k < hs.size(); ++k) {
+        if (status) status[idx[k]] = st[k];
+        if (st[k] == NS3D_OK) ns3d_get_result(hs[k], &results[idx[k]]);
+        ns3d_close(hs[k]);
+    }
+    return worst;
 }
 
 NS3D_API int ns3d_solve_sweep(ns3d_handle *H, const double *gradp, int32_t n, int32_t warm_start,

@@ -1,0 +1,91 @@
+"""Lockstep solves: the SIMPLEC solves of many images (different sizes,
+flow directions and precisions) driven together from one host thread --
+every step for all images at once, the BiCGSTAB steps as merged sets -- give
+each image exactly the result and the logs of its own ns3d_solve."""
+import numpy as np
+import pytest
+
+from helpers import params
+from ns3d_gb300 import capi, synth
+
+pytestmark = pytest.mark.gpu
+
+# shape, radius, porosity, direction, precision
+SPECS = [((20, 16, 18), 3, 0.6, 1, 0), ((24, 20, 16), 2, 0.7, 2, 0), ((16, 22, 20), 3, 0.55, 3, 0),
+         ((18, 18, 24), 2, 0.65, 1, 1), ((22, 14, 20), 3, 0.6, 2, 2), ((28, 24, 22), 3, 0.6, 1, 2)]
+
+
+def _requests(lib):
+    reqs = []
+    for k, (shape, r, phi, direction, precision) in enumerate(SPECS):
+        img, _ = synth.rsa_spheres(shape, r, phi, seed=110 + k)
+        # different outer-iteration caps: some images stop on the cap, others converge
+        p = params(lib, method="SIMPLEC", direction=direction, precision=precision, maxitSIMPLE=40 + 20 * (k % 3),
+                   simpletol=1e-5)
+        reqs.append((p, img))
+    return reqs
+
+
+def _logs(d, direction):
+    out = []
+    for name in ("INFO-%d-case.log" % direction, "RES-%d-case.csv" % direction):
+        out.append([x for x in (d / name).read_text().splitlines() if "terminated in" not in x])
+    return out
+
+
+def test_lockstep_equals_single_solves(gpulib, tmp_path):
+    reqs = _requests(gpulib)
+    alone = []
+    for k, (p, img) in enumerate(reqs):
+        d = tmp_path / ("a%d" % k)
+        d.mkdir()
+        s = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
+        s.set_output(d, "case", False)
+        r = s.solve()
+        alone.append((r, s.fields(), _logs(d, p.direction)))
+        s.close()
+    solvers = []
+    for k, (p, img) in enumerate(reqs):
+        d = tmp_path / ("b%d" % k)
+        d.mkdir()
+        s = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
+        s.set_output(d, "case", False)
+        solvers.append(s)
+    rc, st = capi.solve_lockstep(gpulib, solvers)
+    assert rc == 0 and not st.any(), gpulib.ns3d_last_error()
+    for k, (s, (ra, fa, la)) in enumerate(zip(solvers, alone)):
+        r = s.result()
+        for key in ("K", "RMR", "iterations", "converged", "it_u", "it_v", "it_w", "it_p", "krylov_iterations",
+                    "alpha", "pcnorm"):
+            assert getattr(r, key) == getattr(ra, key), (k, key)
+        for a, b in zip(s.fields(), fa):
+            assert np.array_equal(a, b), k
+        assert _logs(tmp_path / ("b%d" % k), reqs[k][0].direction) == la, k
+        s.close()
+
+
+def test_lockstep_rejects_other_methods(gpulib):
+    (p, img), = _requests(gpulib)[:1]
+    q = params(gpulib, method="IDEAL", maxitSIMPLE=5)
+    a = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
+    b = capi.Solver(gpulib, q, synth.to_raw(img), img.shape)
+    rc, st = capi.solve_lockstep(gpulib, [a, b])
+    assert rc == capi.ERR_ARG and (st == capi.ERR_ARG).all()
+    rc, st = capi.solve_lockstep(gpulib, [a, a])
+    assert rc == capi.ERR_ARG
+    a.close()
+    b.close()
+
+
+def test_batch_lockstep_matches_single_solves(gpulib):
+    reqs = _requests(gpulib)[:4]
+    ks = []
+    for p, img in reqs:
+        s = capi.Solver(gpulib, p, synth.to_raw(img), img.shape)
+        ks.append((s.solve().K, s.result().iterations))
+        s.close()
+    res, st, rc = capi.batch_solve_lockstep(gpulib, [p for p, _ in reqs], [synth.to_raw(img) for _, img in reqs],
+                                            [img.shape for _, img in reqs])
+    assert rc == 0 and not st.any()
+    for r, (k, its) in zip(res, ks):
+        assert r.K == k and r.iterations == its

@@ -47,7 +47,7 @@ def test_oracle_exports_the_solver_symbols(oracle):
                  "ns3d_server_cancel_queued", "ns3d_solve_sweep", "ns3d_group_create", "ns3d_set_group",
                  "ns3d_group_get_stats", "ns3d_group_destroy", "ns3d_server_set_merging",
                  "ns3d_server_group_stats", "ns3d_batch_solve_merged", "ns3d_autotune_enable",
-                 "ns3d_autotune_table"}
+                 "ns3d_autotune_table", "ns3d_solve_lockstep", "ns3d_batch_solve_lockstep"}
     for s in declared_symbols():
         if s not in host_only:
             assert hasattr(oracle, s), s
