@@ -195,3 +195,26 @@ def test_autotune_switch_and_empty_table(gpulib):
     assert capi.autotune_table(gpulib) == ""
     assert lib.ns3d_autotune_table(None, 10) == capi.ERR_ARG
     assert lib.ns3d_autotune_enable(0) == 0 and lib.ns3d_autotune_enable(1) == 0
+
+
+def test_lockstep_and_group_arguments_checked_without_work(gpulib):
+    """The lockstep and group entry points check their arguments before any
+    device work: NULL lists, negative counts and bad lane counts are
+    rejected; an empty lockstep list is a no-op."""
+    import ctypes as C
+    lib = capi._declare_server(gpulib)
+    assert lib.ns3d_solve_lockstep(None, 0, None) == 0
+    assert lib.ns3d_solve_lockstep(None, 2, None) == capi.ERR_ARG
+    assert lib.ns3d_solve_lockstep(None, -1, None) == capi.ERR_ARG
+    hs = (C.c_void_p * 1)(None)
+    st = np.full(1, 7, np.int32)
+    assert lib.ns3d_solve_lockstep(hs, 1, st.ctypes.data_as(C.POINTER(C.c_int32))) == capi.ERR_ARG
+    assert st[0] == capi.ERR_ARG
+    res = (capi.Result * 1)()
+    assert lib.ns3d_batch_solve_lockstep(None, None, None, 0, res, None) == capi.ERR_ARG
+    g = C.c_void_p()
+    assert lib.ns3d_group_create(0, C.byref(g)) == capi.ERR_ARG
+    assert lib.ns3d_group_create(17, C.byref(g)) == capi.ERR_ARG
+    assert lib.ns3d_group_create(1, None) == capi.ERR_ARG
+    assert lib.ns3d_group_get_stats(None, None) == capi.ERR_ARG
+    assert lib.ns3d_set_group(None, None) == capi.ERR_ARG
