@@ -349,9 +349,10 @@ NS3D_API int ns3d_server_stop(ns3d_server *s);
  * chunks.  Every system keeps its own Krylov scalars, reduction order and
  * preconditioner, so each result is bit-identical to the solve alone.
  * Attach with ns3d_set_group before ns3d_solve (NULL detaches); destroy a
- * group only after every solve attached to it returned and every handle
- * that was attached to it was closed.  The solves of a group must run on
- * separate host threads.
+ * group after every solve attached to it returned (ns3d_group_destroy
+ * returns NS3D_ERR_STATE while one runs) and before any handle still
+ * attached to it solves again.  The solves of a group must run on separate
+ * host threads.
  */
 typedef struct ns3d_group ns3d_group;
 typedef struct ns3d_group_stats {

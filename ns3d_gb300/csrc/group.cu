@@ -65,6 +65,14 @@ void SolveGroup::leave() {
     cv_.notify_all();  // a leader waiting for this member stops waiting
 }
 
+bool SolveGroup::busy() {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (members_ > 0 || !pending_.empty()) return true;
+    for (auto &l : lanes_)
+        if (l->busy) return true;
+    return false;
+}
+
 SolveGroup::Stats SolveGroup::stats() {
     std::lock_guard<std::mutex> lk(mu_);
     return stats_;
@@ -244,6 +252,7 @@ NS3D_API int ns3d_group_get_stats(ns3d_group *g, ns3d_group_stats *out) {
 }
 
 NS3D_API int ns3d_group_destroy(ns3d_group *g) {
+    if (g && g->g.busy()) return report_error(NS3D_ERR_STATE, "ns3d_group_destroy: solves of the group are running");
     delete g;
     return NS3D_OK;
 }

@@ -300,6 +300,8 @@ class SolveGroup {
     double window_s = 2e-3;  // longest wait of a leader for the other members
 
     int lanes() const { return (int)lanes_.size(); }
+    // a member is solving or a set is queued or being solved
+    bool busy();
 
   private:
     struct Req;
