@@ -17,6 +17,10 @@ permeability solve; steps cycle through SIMPLEC, SIMPLER (N1=2), SIMPLERR
          pressure(-correction) solves: algorithmic bytes per row-iteration
          (408 B by the fixed (45s+48) formula; the fused phases touch 360 B)
          over the kernel's CUDA-event time
+  merged  a multi-image sample (8 device-generated images, edges 32-48,
+         SIMPLEC capped at 150 outer iterations): one at a time, concurrent
+         streams, merged solve sets and lockstep solves, FP64 and multilevel
+         mixed precision, with the loop-grid autotuner's table
   cpu_baseline  the CPU oracle (the repo's restatement of the reference solver)
          on the first outer iterations of the same solve with every host core,
          scaled to a full solve by BiCGSTAB row-iterations
@@ -362,16 +366,19 @@ def run_batch(capi, lib, n_images, edges, max_concurrent):
                             "K_rel_err_vs_fp64": rel}}
 
 
-# Merged sample (opt-in, --merged): the batch mix above (SIMPLEC, flow x)
-# solved in plain FP64 one image at a time, then as batches of concurrent
-# solves on their own streams (ns3d_batch_solve), with their BiCGSTAB sets
-# merged into shared persistent launches (ns3d_batch_solve_merged), and all
-# driven in lockstep by one host thread (ns3d_batch_solve_lockstep), in plain
-# FP64 and in the serving precision.  The FP64 legs follow the same
-# trajectory bit for bit (fixed-order reductions), so max_outer may cap the
-# outer iterations of every leg alike.
-MERGED_IMAGES = 16
-MERGED_LANES = (1, 2)  # lanes of the solve group (cohorts of ceil(solves / lanes))
+# Merged sample (in the default run, bounded; --no-merged skips it): the
+# batch mix above with edges from MERGED_EDGES (SIMPLEC, flow x), solved in
+# plain FP64 one image at a time, then as batches of concurrent solves on
+# their own streams (ns3d_batch_solve), with their BiCGSTAB sets merged into
+# shared persistent launches (ns3d_batch_solve_merged), and all driven in
+# lockstep by one host thread (ns3d_batch_solve_lockstep), in plain FP64 and
+# in the serving precision.  The FP64 legs follow the same trajectory bit for
+# bit (fixed-order reductions), so MERGED_OUTER caps the outer iterations of
+# every leg alike (the sample takes about half a minute).
+MERGED_IMAGES = 8
+MERGED_EDGES = (32, 48)
+MERGED_OUTER = 150
+MERGED_LANES = (1,)  # lanes of the solve group (cohorts of ceil(solves / lanes))
 
 
 def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
@@ -604,8 +611,11 @@ def run_gpu(args):
                           SERVE_ACTIVE)
     merged = None
     if args.merged and world == 1:
-        merged = run_merged(capi, lib, args.merged_images, tuple(int(x) for x in args.batch_edges.split(",")),
-                            SERVE_ACTIVE)
+        try:
+            merged = run_merged(capi, lib, args.merged_images, tuple(int(x) for x in args.merged_edges.split(",")),
+                                SERVE_ACTIVE, max_outer=args.merged_outer)
+        except Exception as e:  # a failed sample is reported, the bench line still printed
+            merged = {"error": repr(e)}
     line = None
     if rank == 0:
         cpu = None
@@ -664,7 +674,7 @@ def run_gpu(args):
 
 
 def main():
-    global METHODS, MAX_OUTER, PRECISION, SERVE_WINDOW, SERVE_EDGE, SERVE_ACTIVE, SERVE_PRECISION
+    global METHODS, MAX_OUTER, PRECISION, SERVE_WINDOW, SERVE_EDGE, SERVE_ACTIVE, SERVE_PRECISION, MERGED_LANES
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=4)
@@ -679,9 +689,13 @@ def main():
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
-    ap.add_argument("--merged", action="store_true",
-                    help="add the merged-solve-set sample (FP64 batch: one at a time, streams, merged)")
+    ap.add_argument("--no-merged", dest="merged", action="store_false",
+                    help="skip the multi-image sample (one at a time, streams, merged sets, lockstep)")
     ap.add_argument("--merged-images", type=int, default=MERGED_IMAGES)
+    ap.add_argument("--merged-edges", default=",".join(str(e) for e in MERGED_EDGES))
+    ap.add_argument("--merged-outer", type=int, default=MERGED_OUTER)
+    ap.add_argument("--merged-lanes", default=",".join(str(x) for x in MERGED_LANES),
+                    help="lane counts of the merged legs")
     ap.add_argument("--no-mixed-mg", dest="mixed_mg", action="store_false",
                     help="skip the workload's solves in mixed precision with the multilevel preconditioner")
     ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)
@@ -694,6 +708,7 @@ def main():
     ap.add_argument("--max-outer", type=int, default=2000,
                     help="cap on outer iterations (maxitSIMPLE); below 2000 only for short profiling runs")
     args = ap.parse_args()
+    MERGED_LANES = tuple(int(x) for x in args.merged_lanes.split(",") if x.strip())
     SERVE_WINDOW = args.serving_window
     SERVE_EDGE = tuple(int(x) for x in args.serving_edge.split(","))
     SERVE_ACTIVE = args.serving_active
