@@ -21,32 +21,29 @@ struct Scalars {
 
 }  // namespace ns3d
 
-// internal header of the library's translation units (the C-ABI type must
-// live in the global namespace; its members use the library's types)
-using namespace ns3d;
-
 struct ns3d_handle {
     ns3d_params prm;
     int rnx = 0, rny = 0, rnz = 0;  // raw image
     int nx = 0, ny = 0, nz = 0;     // solver frame
     int np = 0, nu = 0, nv = 0, nw = 0;
-    OwnedStream owned_stream;  // destroyed after every buffer freed on it
+    ns3d::OwnedStream owned_stream;  // destroyed after every buffer freed on it
     cudaStream_t stream = nullptr;
 
-    DBuf<uint8_t> img;
-    DBuf<int> pmap, umap, vmap, wmap;
-    DevSys U, V, W, P;
+    ns3d::DBuf<uint8_t> img;
+    ns3d::DBuf<int> pmap, umap, vmap, wmap;
+    ns3d::DevSys U, V, W, P;
     // fields and work vectors (npad of their system)
-    DBuf<double> p, u, v, w, pc, ptemp, utemp, vtemp, wtemp, uh, vh, wh, ut, vt, wt;
-    DBuf<double> diag_part;
-    DBuf<DiagOut> diag;
-    HBuf<DiagOut> h_diag;
-    KrylovSet kmom, kp;
-    MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
-    SolveGroup *group = nullptr;  // sets merged with other solves' (ns3d_set_group)
+    ns3d::DBuf<double> p, u, v, w, pc, ptemp, utemp, vtemp, wtemp, uh, vh, wh, ut, vt, wt;
+    ns3d::DBuf<double> diag_part;
+    ns3d::DBuf<ns3d::DiagOut> diag;
+    ns3d::HBuf<ns3d::DiagOut> h_diag;
+    ns3d::KrylovSet kmom, kp;
+    ns3d::MixedSet mmom, mp;  // FP32 inner / FP64 outer solves (precision = MIXED)
+    ns3d::SolveGroup *group = nullptr;  // sets merged with other solves' (ns3d_set_group)
     bool mixed() const { return prm.precision != NS3D_FP64; }
     // an FP64 set: alone, or merged with the sets of the group's other solves
-    void run_fp64(KrylovSet &own, const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
+    void run_fp64(ns3d::KrylovSet &own, const std::vector<ns3d::SolveItem> &items,
+                  std::vector<ns3d::SolveOutcome> &out) {
         if (!group) {
             own.run(items, stream, out);
             return;
@@ -56,7 +53,7 @@ struct ns3d_handle {
     }
     // a mixed-precision set: alone, or merged (with the preconditioner and
     // FP32 loop variant its own set chooses)
-    void run_mixed(MixedSet &own, std::vector<SolveItem> items, std::vector<SolveOutcome> &out) {
+    void run_mixed(ns3d::MixedSet &own, std::vector<ns3d::SolveItem> items, std::vector<ns3d::SolveOutcome> &out) {
         if (!group) {
             own.run(items, stream, out);
             return;
@@ -65,7 +62,7 @@ struct ns3d_handle {
         for (size_t i = 0; i < items.size(); ++i) items[i].mg = own.uses_mg((int)i);
         group->run_mixed(items, stream, own.out_state_buffer(), out, own.variant());
     }
-    void solve_p(const std::vector<SolveItem> &items, std::vector<SolveOutcome> &out) {
+    void solve_p(const std::vector<ns3d::SolveItem> &items, std::vector<ns3d::SolveOutcome> &out) {
         if (mixed()) run_mixed(mp, items, out);
         else run_fp64(kp, items, out);
     }
@@ -76,21 +73,21 @@ struct ns3d_handle {
     double RMR = 0, old_RMR = 0, deltaRMR, pcmax = 0, pcmin = 0, pcnorm = 0;
     int border;
     std::list<double> avgRMR;
-    SolveOutcome su, sv, sw, sp;
+    ns3d::SolveOutcome su, sv, sw, sp;
 
     ns3d_result res;
     std::string outdir, stem;
     bool write_fields = false, have_out = false;
-    TextLog info, resl;
+    ns3d::TextLog info, resl;
 
-    Grid grid() const {
-        Grid g;
+    ns3d::Grid grid() const {
+        ns3d::Grid g;
         g.nx = nx; g.ny = ny; g.nz = nz;
         g.pmap = pmap.p; g.umap = umap.p; g.vmap = vmap.p; g.wmap = wmap.p;
         return g;
     }
-    Phys phys() const {
-        Phys ph;
+    ns3d::Phys phys() const {
+        ns3d::Phys ph;
         ph.dx = dx; ph.dy = dy; ph.dz = dz; ph.mu = mu; ph.rho = rho; ph.alpha = alpha; ph.beta = beta;
         ph.p0 = p0; ph.p1 = p1; ph.schemefactor = schemefactor;
         ph.idx = 1 / dx; ph.idy = 1 / dy; ph.idz = 1 / dz;
@@ -108,39 +105,40 @@ struct ns3d_handle {
     // the steps split where the lockstep driver solves or reads back for
     // many instances at once (the whole steps are these parts in order)
     void begin_solve();
-    std::vector<SolveItem> momentum_items();             // the u, v (, w) systems
-    std::vector<SolveItem> pressure_correction_items();  // the pc system
-    std::vector<SolveItem> velocity_begin();
-    void velocity_end(const std::vector<SolveOutcome> &out, bool limit, double dvmax);
-    std::vector<SolveItem> pressure_correction_begin();
-    void pressure_correction_end(const std::vector<SolveOutcome> &out);
+    std::vector<ns3d::SolveItem> momentum_items();             // the u, v (, w) systems
+    std::vector<ns3d::SolveItem> pressure_correction_items();  // the pc system
+    std::vector<ns3d::SolveItem> velocity_begin();
+    void velocity_end(const std::vector<ns3d::SolveOutcome> &out, bool limit, double dvmax);
+    std::vector<ns3d::SolveItem> pressure_correction_begin();
+    void pressure_correction_end(const std::vector<ns3d::SolveOutcome> &out);
     void correct_pressure_launch();
     void correct_pressure_read();
     void permeability_launch();
-    void permeability_read(Scalars &s);
+    void permeability_read(ns3d::Scalars &s);
     void divergence_launch();
-    void divergence_read(Scalars &s);
-    void diagnostics_end(Scalars &s);
-    void log_solve(const char *comp, const SolveOutcome &o);
-    void log_pressure_status(const SolveOutcome &o);
+    void divergence_read(ns3d::Scalars &s);
+    void diagnostics_end(ns3d::Scalars &s);
+    void log_solve(const char *comp, const ns3d::SolveOutcome &o);
+    void log_pressure_status(const ns3d::SolveOutcome &o);
     void compute_pressure_correction();
     void compute_pressure_field();
     void correct_pressure_field();
-    void permeability(Scalars &s);
-    void divergence(Scalars &s);
-    void diagnostics(Scalars &s);
+    void permeability(ns3d::Scalars &s);
+    void divergence(ns3d::Scalars &s);
+    void diagnostics(ns3d::Scalars &s);
     void relax_control(bool beta_cst);
     bool check_convergence(double res_, double tol) const;
     void pressure_step(bool relax_p, const double *uc, const double *vc, const double *wc, const double *uold,
                        const double *vold, const double *wold, double *ux, double *vx, double *wx);
     void hats(const double *uc, const double *vc, const double *wc, const double *uold, const double *vold,
               const double *wold);
-    void res_row(int it, const Scalars &s);
+    void res_row(int it, const ns3d::Scalars &s);
     void fields_to_image(const std::string &file);
     void save_snapshot(int it, int &savecounter);
     void header(const char *name, const char *maxname);
-    void finish(const char *name, int it, const Scalars &s, std::chrono::steady_clock::time_point t0, time_t start);
-    void initial_velocity(Scalars &s);
+    void finish(const char *name, int it, const ns3d::Scalars &s, std::chrono::steady_clock::time_point t0,
+                time_t start);
+    void initial_velocity(ns3d::Scalars &s);
     void run_simplec();
     void run_simpler_family(int method);
     void old_rmr_update(int it) {
