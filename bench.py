@@ -21,6 +21,8 @@ permeability solve; steps cycle through SIMPLEC, SIMPLER (N1=2), SIMPLERR
          SIMPLEC capped at 150 outer iterations): one at a time, concurrent
          streams, merged solve sets and lockstep solves, FP64 and multilevel
          mixed precision, with the loop-grid autotuner's table
+  readme_64  the reference's published benchmark case (its README's 64^3
+         four-method table) solved here, beside the published CPU times
   cpu_baseline  the CPU oracle (the repo's restatement of the reference solver)
          on the first outer iterations of the same solve with every host core,
          scaled to a full solve by BiCGSTAB row-iterations
@@ -450,6 +452,41 @@ def run_merged(capi, lib, n_images, edges, max_concurrent, max_outer=2000):
     return legs
 
 
+# The reference's own published benchmark (README.md:181-187 of
+# jerome-lux/NS3D): tests/compare_algorithms.ini on data/spheres_64.vti (a
+# regular 64^3 sphere lattice, regenerated here byte for byte), the four
+# methods, wall times on an unstated CPU with 4 OpenMP threads.  Each method
+# is solved here in plain FP64 (image upload, geometry build and solve
+# timed together; the reference's times also include reading the file).
+README_64 = {"SIMPLEC": (3.28386e-12, 48, 5.435), "SIMPLER": (3.28382e-12, 42, 8.033),
+             "SIMPLERR": (3.28175e-12, 23, 5.690), "IDEAL": (3.28212e-12, 19, 2.788)}
+
+
+def readme64_params(capi, lib, method):
+    return capi.default_params(lib, dx=2e-6, dy=-1.0, dz=-1.0, mu=1e-3, rho=1e3, p0=1e5, gradp=1e2, alpha=0.8,
+                               beta=1.0, vsolvertol=1e-5, psolvertol=1e-6, pcsolvertol=1e-3, simpletol=1e-4,
+                               deltaRMR=1e-4, maxitsolver=500, maxitSIMPLE=200, N1=2, N2=2, porevalue=0,
+                               direction=1, border=0, method=method, precision=0)
+
+
+def run_readme64(capi, lib):
+    from ns3d_gb300 import synth
+    img = synth.sphere_lattice(64, 8, 3)
+    raw = synth.to_raw(img)
+    out = {"case": "README 64^3 compare_algorithms table (sphere lattice, 4 methods), plain FP64",
+           "published_hardware": "CPU, 4 OpenMP threads (model unstated)"}
+    for m, (k_pub, it_pub, sec_pub) in README_64.items():
+        t = time.perf_counter()
+        s = capi.Solver(lib, readme64_params(capi, lib, m), raw, img.shape)
+        r = s.solve()
+        dt = time.perf_counter() - t
+        s.close()
+        out[m] = {"seconds": dt, "K": r.K, "outer_iterations": int(r.iterations), "converged": int(r.converged),
+                  "published_seconds": sec_pub, "published_K": k_pub, "published_iterations": it_pub,
+                  "K_rel_diff_vs_published": abs(r.K - k_pub) / k_pub, "speedup_vs_published": sec_pub / dt}
+    return out
+
+
 # Large sample (opt-in, --large): a 256^3 image of isotropic
 # straight fibres of radius 3, porosity ~0.85, seed 2, flow along z --
 # generated on the device; the first LARGE_OUTER outer SIMPLEC iterations in
@@ -609,6 +646,12 @@ def run_gpu(args):
     if args.batch and world == 1:
         batch = run_batch(capi, lib, args.batch_images, tuple(int(x) for x in args.batch_edges.split(",")),
                           SERVE_ACTIVE)
+    readme64 = None
+    if args.readme64 and world == 1:
+        try:
+            readme64 = run_readme64(capi, lib)
+        except Exception as e:  # a failed sample is reported, the bench line still printed
+            readme64 = {"error": repr(e)}
     merged = None
     if args.merged and world == 1:
         try:
@@ -663,6 +706,7 @@ def run_gpu(args):
                 "serving": serving,
                 "batch": batch,
                 "merged": merged,
+                "readme_64": readme64,
                 "large": large,
                 "clocks": clk}
         print(json.dumps(line))
@@ -689,6 +733,8 @@ def main():
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--batch", action="store_true", help="add the batch sample (opt-in: a few minutes)")
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
+    ap.add_argument("--no-readme64", dest="readme64", action="store_false",
+                    help="skip the reference's published 64^3 four-method case")
     ap.add_argument("--no-merged", dest="merged", action="store_false",
                     help="skip the multi-image sample (one at a time, streams, merged sets, lockstep)")
     ap.add_argument("--merged-images", type=int, default=MERGED_IMAGES)
