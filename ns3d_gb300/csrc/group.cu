@@ -1,16 +1,16 @@
 // group.cu -- merged solve sets: the BiCGSTAB work of many concurrent solves
 // in one set of persistent kernels (SolveGroup, runtime.h), and its C-ABI.
 //
-// A member thread queues its set and waits; the first waiting member whose
-// set is still queued becomes the leader: it waits until every member that
-// is solving has queued a set (or window_s passes), takes the oldest queued
-// set and the later ones of the same kind in arrival order, up to the
-// merged capacity (KMAX_MERGED FP64 or KMAX_MERGED_M mixed systems), orders
-// the group stream after each member's stream (an event per set), runs the
-// merged set, copies each system's final state back to its member, and
-// orders each member's stream after the merged launch (a second event per
-// set).  Leaders take turns, one at a time, so the group stream and its sets
-// have a single user.
+// A member thread queues its set and waits.  A waiting member whose set is
+// still queued becomes the leader of a free lane: it waits until a cohort
+// of sets is queued (ceil(members / lanes), or window_s passes), takes the
+// oldest queued set and the later ones of the same kind in arrival order,
+// up to the cohort and the merged capacity (KMAX_MERGED FP64 or
+// KMAX_MERGED_M mixed systems), orders the lane's stream after each
+// member's stream (an event per set), runs the merged set, copies each
+// system's final state back to its member, and orders each member's stream
+// after the merged launch (a second event per set).  A lane has one leader
+// at a time, so its stream and its sets have a single user.
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -43,16 +43,16 @@ SolveGroup::SolveGroup(int lanes) {
     }
 }
 
-SolveGroup::~SolveGroup() {
-    for (auto &l : lanes_) {
-        l->set.reset();  // their buffers are freed on the lane's stream
-        l->mset.reset();
-        if (l->stream) {
-            cudaStreamSynchronize(l->stream);
-            cudaStreamDestroy(l->stream);
-        }
+SolveGroup::Lane::~Lane() {
+    set.reset();  // their buffers are freed on the lane's stream
+    mset.reset();
+    if (stream) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
     }
 }
+
+SolveGroup::~SolveGroup() = default;
 
 void SolveGroup::join() {
     std::lock_guard<std::mutex> lk(mu_);

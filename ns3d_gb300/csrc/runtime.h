@@ -310,6 +310,7 @@ class SolveGroup {
         std::unique_ptr<KrylovSetMerged> set;
         std::unique_ptr<MixedSetMerged> mset;
         bool busy = false;
+        ~Lane();  // frees the sets' buffers on the stream, then the stream
     };
     void submit(Req &r);
     void execute(Lane &lane, std::vector<Req *> &batch);
