@@ -270,12 +270,16 @@ NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
  * multiple of 1024 and >= n), the right-hand side and the guess/solution x
  * (npad doubles each) and a CUDA stream (NULL = default stream).  Work vectors
  * live in a fixed device array inside the library: at most 65536 rows
- * (larger n returns NS3D_ERR_ARG); the array (about 4.5 MiB) is held on every
- * GPU that loads the library until exit.  The first call on a device looks
- * up the array's device address (cudaGetSymbolAddress), so make it before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race and must be serialized by the caller.  Same arithmetic and results as
- * ns3d_solve_system.  Error text: ns3d_noalloc_last_error().
+ * (larger n returns NS3D_ERR_ARG); the array (about 4.5 MiB) is held until
+ * exit.  CUDA loads a library's device code lazily by default, so the array
+ * (and the kernels' code) are placed on a device by the first call on that
+ * device, which also looks up the array's device address
+ * (cudaGetSymbolAddress): make that first call before the host reserves the
+ * rest of the device's memory and before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be serialized
+ * by the caller.  Same arithmetic and results as ns3d_solve_system.  Error
+ * text: ns3d_noalloc_last_error() (the text of this thread's last failed
+ * call; a successful call clears it).
  */
 NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t *nbr, const double *rhs, double *x, int32_t n,
                                    int32_t npad, double tol, int32_t maxit, void *stream, ns3d_solve_info *info);
@@ -350,8 +354,11 @@ NS3D_API int ns3d_server_stop(ns3d_server *s);
  * preconditioner, so each result is bit-identical to the solve alone.
  * Attach with ns3d_set_group before ns3d_solve (NULL detaches); destroy a
  * group after every solve attached to it returned (ns3d_group_destroy
- * returns NS3D_ERR_STATE while one runs) and before any handle still
- * attached to it solves again.  The solves of a group must run on separate
+ * returns NS3D_ERR_STATE while one runs; a solve that starts while the
+ * destroy runs fails with NS3D_ERR_STATE) and before any handle still
+ * attached to it solves again.  The caller must make sure that no thread can
+ * still reach the group (attach, solve) once ns3d_group_destroy returned OK:
+ * the group's memory is freed.  The solves of a group must run on separate
  * host threads.
  */
 typedef struct ns3d_group ns3d_group;

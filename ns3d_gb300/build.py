@@ -1,7 +1,9 @@
 """Build recipe of the NS3D GB300 library (no cmake, a minute or two).
 
-Compiles the CUDA translation units for sm_103a only (FP64 files with
---fmad=false: the arithmetic contract of the kernels), the host C++ files,
+Compiles the CUDA translation units for sm_103a only (--fmad=false: the
+arithmetic contract of the kernels; host code everywhere with
+-ffp-contract=off, so the scalar control arithmetic on the host rounds as
+written on x86-64 and on Arm alike), the host C++ files,
 links libns3d_gb300.so in-tree under ns3d_gb300/_lib/ and the NS3D program
 beside it.  Objects go to ns3d_gb300/_build/.
 """
@@ -60,7 +62,7 @@ def build(verbose=False, ptxas_info=False):
         objs.append(obj)
         if _stale(obj, [src] + headers):
             cmd = [nvcc] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "--fmad=false", "--extended-lambda",
-                                   "-Xcompiler", "-fPIC,-fvisibility=hidden", "-c", src, "-o", obj]
+                                   "-Xcompiler", "-fPIC,-fvisibility=hidden,-ffp-contract=off", "-c", src, "-o", obj]
             if ptxas_info:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)
@@ -70,7 +72,8 @@ def build(verbose=False, ptxas_info=False):
         objs.append(obj)
         if _stale(obj, [src] + headers):
             cuda_inc = os.path.join(os.path.dirname(os.path.dirname(nvcc)), "include")
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-Wall", "-pthread",
+            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-fvisibility=hidden", "-ffp-contract=off", "-Wall",
+                         "-pthread",
                          "-I" + cuda_inc, "-c", src, "-o", obj])
     with cf.ThreadPoolExecutor(max_workers=max(1, min(len(jobs), os.cpu_count() or 4))) as ex:
         outs = list(ex.map(_run, jobs))

@@ -56,6 +56,7 @@ SolveGroup::~SolveGroup() = default;
 
 void SolveGroup::join() {
     std::lock_guard<std::mutex> lk(mu_);
+    if (closing_) throw ApiError(NS3D_ERR_STATE, "the solve group is being destroyed");
     members_++;
 }
 
@@ -71,6 +72,15 @@ bool SolveGroup::busy() {
     for (auto &l : lanes_)
         if (l->busy) return true;
     return false;
+}
+
+bool SolveGroup::close_if_idle() {
+    std::lock_guard<std::mutex> lk(mu_);
+    if (members_ > 0 || !pending_.empty()) return false;
+    for (auto &l : lanes_)
+        if (l->busy) return false;
+    closing_ = true;
+    return true;
 }
 
 SolveGroup::Stats SolveGroup::stats() {
@@ -252,7 +262,8 @@ NS3D_API int ns3d_group_get_stats(ns3d_group *g, ns3d_group_stats *out) {
 }
 
 NS3D_API int ns3d_group_destroy(ns3d_group *g) {
-    if (g && g->g.busy()) return report_error(NS3D_ERR_STATE, "ns3d_group_destroy: solves of the group are running");
+    if (g && !g->g.close_if_idle())
+        return report_error(NS3D_ERR_STATE, "ns3d_group_destroy: solves of the group are running");
     delete g;
     return NS3D_OK;
 }

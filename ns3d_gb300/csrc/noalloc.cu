@@ -14,7 +14,10 @@
 // Host code cannot use the array's name as a device address (it names a
 // host-side stand-in), so the first call on each device looks the address up
 // with cudaGetSymbolAddress while that device is current, checks the result
-// and caches it; that first call should come before any stream capture.
+// and caches it.  Under CUDA's default lazy module loading this lookup is
+// also what places the array (and this module's code) on the device, so the
+// first call should come before the host reserves the rest of the device's
+// memory, and before any stream capture.
 // Every call shares the one array and overwrites it: calls that overlap on
 // the GPU (two streams, two host threads) race, so serialize them.
 #include <cstring>
@@ -84,6 +87,7 @@ extern "C" NS3D_API const char *ns3d_noalloc_last_error(void) { return g_noalloc
 extern "C" NS3D_API int ns3d_bicgstab_noalloc(const double *coef, const int32_t *nbr, const double *rhs, double *x,
                                               int32_t n, int32_t npad, double tol, int32_t maxit, void *stream,
                                               ns3d_solve_info *info) {
+    g_noalloc_err = "";  // the text describes this call's failure only
     if (!coef || !nbr || !rhs || !x || !info) return fail(NS3D_ERR_ARG, "NULL argument");
     if (n < 0 || maxit <= 0 || !(tol >= 0)) return fail(NS3D_ERR_ARG, "bad size, tolerance or iteration cap");
     if (n > kScratchRows) return fail(NS3D_ERR_ARG, "system larger than the 65536-row scratch of this entry point");

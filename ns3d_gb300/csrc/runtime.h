@@ -302,6 +302,12 @@ class SolveGroup {
     int lanes() const { return (int)lanes_.size(); }
     // a member is solving or a set is queued or being solved
     bool busy();
+    // Marks the group closed if it is idle (under the group's lock, so no
+    // solve can join between the check and the mark) and returns true;
+    // false while it is busy.  join() of a closed group throws
+    // NS3D_ERR_STATE.  Threads that still hold the group after it is
+    // destroyed are the caller's to prevent.
+    bool close_if_idle();
 
   private:
     struct Req;
@@ -318,6 +324,7 @@ class SolveGroup {
     std::condition_variable cv_;
     std::deque<Req *> pending_;
     int members_ = 0;
+    bool closing_ = false;  // set by close_if_idle: the group is being destroyed
     Stats stats_;
     std::vector<std::unique_ptr<Lane>> lanes_;
 };

@@ -1,5 +1,6 @@
 """Generate tests/golden/reference_runs.json from the reference's own
-published results (run once where the reference checkout is available).
+published results (run once where the reference checkout is available;
+the checkout's root is the first argument, or NS3D_REFERENCE_ROOT).
 
 Sources (paths inside the reference project):
   tests/results/RES-1-spheres_128.csv   per-iteration RES rows of test_spheres.ini
@@ -20,7 +21,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.dirname(HERE))
 import vtiutil  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("NS3D_REFERENCE_ROOT")
 
 
 def ini(path):
@@ -34,6 +35,8 @@ def ini(path):
 
 
 def main():
+    if not REF:
+        sys.exit("usage: make_golden.py <reference root> (or set NS3D_REFERENCE_ROOT)")
     res_lines = open(os.path.join(REF, "tests/results/RES-1-spheres_128.csv")).read().splitlines()
     header = res_lines[0]
     rows = []

@@ -176,10 +176,12 @@ def test_vti_errors(gpulib, tmp_path):
 
 
 def test_golden_fields_decode(gpulib):
-    """The reference's golden outputs decode to the documented shapes."""
-    ref = "/root/reference/tests/results/P-1-spheres_128.vti"
-    if not os.path.exists(ref):
-        pytest.skip("reference checkout not present")
+    """The reference's golden outputs decode to the documented shapes (needs
+    the reference checkout: its root in NS3D_REFERENCE_ROOT)."""
+    root = os.environ.get("NS3D_REFERENCE_ROOT")
+    if not root:
+        pytest.skip("NS3D_REFERENCE_ROOT not set")
+    ref = os.path.join(root, "tests", "results", "P-1-spheres_128.vti")
     p = ns.read_vti_f64(ref)
     assert p.shape == (128, 128, 128)
     u = ns.read_vti_f64(ref.replace("P-1", "Vx-1"))
