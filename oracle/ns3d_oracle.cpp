@@ -126,6 +126,46 @@ double det_dot(const std::vector<double> &a, const std::vector<double> &b, long 
     return det_sum(n, [&](long r, double acc) { return std::fma(pa[r], pb[r], acc); });
 }
 
+/*
+ * Alternative rounding of the BiCGSTAB arithmetic, for experiments only
+ * (environment variable NS3D_ORACLE_ARITH, read when a solver opens; unset
+ * or "fixed" = the documented contract above, which the CUDA path follows):
+ *   "serial"   every product rounded before its add, dot products summed
+ *              row 0..n-1 with one accumulator, sparse rows in ascending
+ *              column order (what a scalar build of a sparse library does)
+ *   "packet4"  as "serial" but dot products with 4 interleaved accumulators
+ *              combined pairwise at the end (a 4-wide SIMD reduction)
+ * They exist to measure how much a solve's trajectory depends on rounding
+ * alone (the reference's Eigen reduction order cannot be reproduced).
+ */
+int g_arith = 0;
+
+void read_arith_mode() {
+    const char *e = getenv("NS3D_ORACLE_ARITH");
+    g_arith = 0;
+    if (e && !strcmp(e, "serial")) g_arith = 1;
+    else if (e && !strcmp(e, "packet4")) g_arith = 2;
+}
+
+double alt_dot(const std::vector<double> &a, const std::vector<double> &b, long n) {
+    if (g_arith == 1) {
+        double acc = 0.0;
+        for (long r = 0; r < n; ++r) acc = acc + a[(size_t)r] * b[(size_t)r];
+        return acc;
+    }
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    long r = 0;
+    for (; r + 4 <= n; r += 4)
+        for (int k = 0; k < 4; ++k) acc[k] = acc[k] + a[(size_t)(r + k)] * b[(size_t)(r + k)];
+    double t = (acc[0] + acc[2]) + (acc[1] + acc[3]);
+    for (; r < n; ++r) t = t + a[(size_t)r] * b[(size_t)r];
+    return t;
+}
+
+inline double bdot(const std::vector<double> &a, const std::vector<double> &b, long n) {
+    return g_arith == 0 ? det_dot(a, b, n) : alt_dot(a, b, n);
+}
+
 /* std::min(F,0.0) / std::max(F,0.0) exactly as the standard library selects */
 inline double min0(double F) { return (0.0 < F) ? 0.0 : F; }
 inline double max0(double F) { return (F < 0.0) ? 0.0 : F; }
@@ -181,6 +221,15 @@ struct System {
     inline double val(int e, int r) const { return c[slot[(size_t)e]][(size_t)r]; }
     // y = A x, each row summed with fma in ascending column order
     void spmv(const std::vector<double> &x, std::vector<double> &y) const {
+        if (g_arith != 0) {  // experiments: products rounded before the adds
+#pragma omp parallel for schedule(static)
+            for (int r = 0; r < n; ++r) {
+                double t = 0.0;
+                for (int e = rp[(size_t)r]; e < rp[(size_t)r + 1]; ++e) t = t + val(e, r) * x[(size_t)col[(size_t)e]];
+                y[(size_t)r] = t;
+            }
+            return;
+        }
 #pragma omp parallel for schedule(static)
         for (int r = 0; r < n; ++r) {
             double t = 0.0;
@@ -234,8 +283,8 @@ SolveOut bicgstab(const System &A, const std::vector<double> &b, std::vector<dou
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < n; ++i) r[(size_t)i] = b[(size_t)i] - ax[(size_t)i];
     r0 = r;
-    double r0_sqnorm = det_dot(r0, r0, n);
-    double rhs_sqnorm = det_dot(b, b, n);
+    double r0_sqnorm = bdot(r0, r0, n);
+    double rhs_sqnorm = bdot(b, b, n);
     if (rhs_sqnorm == 0.0) {
         std::fill(x.begin(), x.end(), 0.0);
         out.iters = maxit;
@@ -248,47 +297,53 @@ SolveOut bicgstab(const System &A, const std::vector<double> &b, std::vector<dou
     const double eps2 = DBL_EPSILON * DBL_EPSILON;
     long i = 0;
     int restarts = 0;
-    double rr = det_dot(r, r, n);
+    double rr = bdot(r, r, n);
     const double *iv = A.invdiag.data();
     while (rr > tol2 && i < maxit) {
         double rho_old = rho;
-        rho = det_dot(r0, r, n);
+        rho = bdot(r0, r, n);
         if (std::fabs(rho) < eps2 * r0_sqnorm) {
             A.spmv(x, ax);
 #pragma omp parallel for schedule(static)
             for (long k = 0; k < n; ++k) r[(size_t)k] = b[(size_t)k] - ax[(size_t)k];
             r0 = r;
-            rho = r0_sqnorm = det_dot(r, r, n);
+            rho = r0_sqnorm = bdot(r, r, n);
             if (restarts++ == 0) i = 0;
         }
         double beta = (rho / rho_old) * (alpha / w);
 #pragma omp parallel for schedule(static)
         for (long k = 0; k < n; ++k) {
-            double pk = std::fma(beta, std::fma(-w, v[(size_t)k], p[(size_t)k]), r[(size_t)k]);
+            double pk = g_arith ? r[(size_t)k] + beta * (p[(size_t)k] - w * v[(size_t)k])
+                                : std::fma(beta, std::fma(-w, v[(size_t)k], p[(size_t)k]), r[(size_t)k]);
             p[(size_t)k] = pk;
             y[(size_t)k] = iv[k] * pk;
         }
         A.spmv(y, v);
-        alpha = rho / det_dot(r0, v, n);
+        alpha = rho / bdot(r0, v, n);
 #pragma omp parallel for schedule(static)
         for (long k = 0; k < n; ++k) {
-            double sk = std::fma(-alpha, v[(size_t)k], r[(size_t)k]);
+            double sk = g_arith ? r[(size_t)k] - alpha * v[(size_t)k] : std::fma(-alpha, v[(size_t)k], r[(size_t)k]);
             s[(size_t)k] = sk;
             z[(size_t)k] = iv[k] * sk;
         }
         A.spmv(z, t);
-        double tmp = det_dot(t, t, n);
-        double ts = det_dot(t, s, n);
+        double tmp = bdot(t, t, n);
+        double ts = bdot(t, s, n);
         if (tmp > 0.0)
             w = ts / tmp;
         else
             w = 0.0;
 #pragma omp parallel for schedule(static)
         for (long k = 0; k < n; ++k) {
-            x[(size_t)k] = std::fma(w, z[(size_t)k], std::fma(alpha, y[(size_t)k], x[(size_t)k]));
-            r[(size_t)k] = std::fma(-w, t[(size_t)k], s[(size_t)k]);
+            if (g_arith) {
+                x[(size_t)k] = x[(size_t)k] + (alpha * y[(size_t)k] + w * z[(size_t)k]);
+                r[(size_t)k] = s[(size_t)k] - w * t[(size_t)k];
+            } else {
+                x[(size_t)k] = std::fma(w, z[(size_t)k], std::fma(alpha, y[(size_t)k], x[(size_t)k]));
+                r[(size_t)k] = std::fma(-w, t[(size_t)k], s[(size_t)k]);
+            }
         }
-        rr = det_dot(r, r, n);
+        rr = bdot(r, r, n);
         ++i;
         ++out.work;
         if (krylov_rows) *krylov_rows += n;
@@ -1622,6 +1677,7 @@ NS3D_API void ns3d_params_default(ns3d_params *p) {
 NS3D_API int ns3d_open(const ns3d_params *params, const uint8_t *raw, int32_t nx, int32_t ny, int32_t nz,
                        ns3d_handle **out) {
     if (!params || !raw || !out) return fail(NS3D_ERR_ARG, "ns3d_open: NULL argument");
+    read_arith_mode();
     if (nx <= 0 || ny <= 0 || nz <= 0) return fail(NS3D_ERR_ARG, "ns3d_open: bad image size");
     if ((long)nx * ny * nz > 0x7fffffffL) return fail(NS3D_ERR_ARG, "ns3d_open: image too large");
     if (params->direction < 1 || params->direction > 3) return fail(NS3D_ERR_ARG, "ns3d_open: direction must be 1, 2 or 3");
