@@ -137,7 +137,10 @@ NS3D_API void ns3d_params_default(ns3d_params *p);
  * Build a solver instance from a raw voxel image.
  * raw: nx*ny*nz bytes in VTK order (x fastest), as read from the .vti file
  *      (readvtkfile_uint8, src/vtkio.cxx:96-150): a voxel equal to
- *      params->porevalue is fluid.
+ *      params->porevalue is fluid.  Host memory, or device memory of the
+ *      current device (the copy direction follows the pointer).
+ * A parameter that is NaN or infinite returns NS3D_ERR_ARG before any device
+ * work (the reference would carry it into every field).
  * The image is binarized, rotated so the flow runs along x
  * (NavierStokesBase::Rotation, src/NSBase.cxx:2451-2492), padded along x
  * (AddBorder, src/NSBase.cxx:2425-2448) and indexed
@@ -162,12 +165,15 @@ NS3D_API int ns3d_get_index_arrays(ns3d_handle *h, int32_t *pindex, int32_t *uin
  * Initial fields, image-shaped in the rotated frame (p: nx*ny*nz,
  * u: (nx+1)*ny*nz, v,w: nx*ny*nz).  NULL keeps the default: the linear
  * pressure profile p0 + (p1-p0)(i+1)/nx (Initpvector, src/NSBase.cxx:2645-2690)
- * and zero velocity (InitVelocity, src/NSBase.cxx:2575-2642).
+ * and zero velocity (InitVelocity, src/NSBase.cxx:2575-2642).  A NaN or an
+ * infinity anywhere in a given array returns NS3D_ERR_ARG and leaves the
+ * fields unchanged.
  */
 NS3D_API int ns3d_set_initial_fields(ns3d_handle *h, const double *p_img, const double *u_img,
                                      const double *v_img, const double *w_img);
 
-/* Compacted fields (lengths np, nu, nv, nw).  Any pointer may be NULL. */
+/* Compacted fields (lengths np, nu, nv, nw).  Any pointer may be NULL.
+ * ns3d_set_fields rejects non-finite values like ns3d_set_initial_fields. */
 NS3D_API int ns3d_get_fields(ns3d_handle *h, double *p, double *u, double *v, double *w);
 NS3D_API int ns3d_set_fields(ns3d_handle *h, const double *p, const double *u,
                              const double *v, const double *w);
@@ -255,10 +261,13 @@ typedef struct ns3d_profile {
     int64_t launches[6];
     double ms[6];
     int64_t rows[6];
-    int64_t total_launches;   /* every kernel launched by this handle */
+    int64_t total_launches;   /* kernels the library launched since profiling was enabled on this handle */
 } ns3d_profile;
 NS3D_API int ns3d_set_profiling(ns3d_handle *h, int32_t enable);
 NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
+/* kernels this library launched in the process so far (every handle,
+ * server and batch call) */
+NS3D_API int64_t ns3d_kernel_launches(void);
 
 /*
  * BiCGSTAB that allocates nothing.  No counterpart in the reference: it
@@ -332,6 +341,11 @@ NS3D_API int ns3d_server_start(int32_t max_active, size_t hbm_budget_bytes, ns3d
 /* keep_fields != 0 keeps the compacted fields for ns3d_server_fields */
 NS3D_API int ns3d_server_submit(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx, int32_t ny,
                                 int32_t nz, int32_t keep_fields, int64_t *ticket);
+/* The same without copying the image: raw (host memory, or device memory of
+ * the server's device -- an image generated or staged there) must stay valid
+ * and unchanged until the request has finished or failed. */
+NS3D_API int ns3d_server_submit_resident(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx,
+                                         int32_t ny, int32_t nz, int32_t keep_fields, int64_t *ticket);
 /* state: 0 queued, 1 running, 2 done, 3 failed (the return value is the failure status) */
 NS3D_API int ns3d_server_poll(ns3d_server *s, int64_t ticket, int32_t *state, ns3d_result *result);
 NS3D_API int ns3d_server_wait(ns3d_server *s, int64_t ticket, ns3d_result *result, double *latency_s);
@@ -407,6 +421,19 @@ NS3D_API int ns3d_batch_solve_lockstep(const ns3d_params *params, const uint8_t 
  */
 NS3D_API int ns3d_autotune_enable(int32_t mode);
 NS3D_API int ns3d_autotune_table(char *buf, int32_t cap);
+
+/*
+ * Testing aid for the failure path of the persistent solver kernels (no
+ * counterpart in the reference, which has no device code).  Their grid-wide
+ * barriers wait a bounded time: after the limit a kernel sets an error flag,
+ * stops, and the call that launched it returns NS3D_ERR_TIMEOUT with the
+ * context intact.  While extra_arrivals > 0, every barrier of every loop-kernel
+ * launch in the process waits for that many arrivals beyond the grid's own,
+ * which never come, and gives up after limit_s seconds (> 0, at most 10), so
+ * a test can watch that path end without a fault.  extra_arrivals = 0
+ * restores normal launches.  Not for use while other solves run.
+ */
+NS3D_API int ns3d_debug_barrier_timeout(int32_t extra_arrivals, double limit_s);
 /* ns3d_batch_solve with the solves merged in a group of `lanes` lanes;
  * stats (may be NULL) of the group */
 NS3D_API int ns3d_batch_solve_merged(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,

@@ -92,6 +92,8 @@ def _declare(lib):
     if hasattr(lib, "ns3d_set_profiling"):
         sig["ns3d_set_profiling"] = (C.c_int, [C.c_void_p, C.c_int32])
         sig["ns3d_get_profile"] = (C.c_int, [C.c_void_p, _P(Profile)])
+    if hasattr(lib, "ns3d_kernel_launches"):
+        sig["ns3d_kernel_launches"] = (C.c_int64, [])
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res
@@ -130,13 +132,18 @@ class Solver:
     """One solver instance (the C handle) on a given library."""
 
     def __init__(self, lib, params, raw_xfastest, dims):
+        """raw_xfastest: the image as a numpy array, or the integer address of
+        nx*ny*nz bytes in host or device memory."""
         self.lib = lib
         self.params = params
-        raw = np.ascontiguousarray(raw_xfastest, dtype=np.uint8).reshape(-1)
-        assert raw.size == dims[0] * dims[1] * dims[2]
+        if isinstance(raw_xfastest, int):
+            ptr = C.cast(C.c_void_p(raw_xfastest), _P(C.c_uint8))
+        else:
+            raw = np.ascontiguousarray(raw_xfastest, dtype=np.uint8).reshape(-1)
+            assert raw.size == dims[0] * dims[1] * dims[2]
+            ptr = _ptr(raw, C.c_uint8)
         h = C.c_void_p()
-        self._check(lib.ns3d_open(C.byref(params), _ptr(raw, C.c_uint8), int(dims[0]), int(dims[1]),
-                                  int(dims[2]), C.byref(h)))
+        self._check(lib.ns3d_open(C.byref(params), ptr, int(dims[0]), int(dims[1]), int(dims[2]), C.byref(h)))
         self.h = h
         s = Sizes()
         self._check(lib.ns3d_get_sizes(h, C.byref(s)))
@@ -280,6 +287,8 @@ def _declare_server(lib):
         "ns3d_server_start": (C.c_int, [C.c_int32, C.c_size_t, _P(C.c_void_p)]),
         "ns3d_server_submit": (C.c_int, [C.c_void_p, _P(Params), _P(C.c_uint8), C.c_int32, C.c_int32, C.c_int32,
                                          C.c_int32, _P(C.c_int64)]),
+        "ns3d_server_submit_resident": (C.c_int, [C.c_void_p, _P(Params), C.c_void_p, C.c_int32, C.c_int32,
+                                                  C.c_int32, C.c_int32, _P(C.c_int64)]),
         "ns3d_server_poll": (C.c_int, [C.c_void_p, C.c_int64, _P(C.c_int32), _P(Result)]),
         "ns3d_server_wait": (C.c_int, [C.c_void_p, C.c_int64, _P(Result), _P(C.c_double)]),
         "ns3d_server_fields": (C.c_int, [C.c_void_p, C.c_int64, _d, _d, _d, _d]),
@@ -336,6 +345,16 @@ class Server:
         t = C.c_int64()
         rc = self.lib.ns3d_server_submit(self.h, C.byref(params), _ptr(raw, C.c_uint8), int(dims[0]), int(dims[1]),
                                          int(dims[2]), int(bool(keep_fields)), C.byref(t))
+        if rc != 0:
+            raise NS3DError(rc, "submit failed")
+        return t.value
+
+    def submit_resident(self, params, raw_ptr, dims, keep_fields=False):
+        """ns3d_server_submit_resident: `raw_ptr` (an integer address, host or
+        device memory) is not copied and must stay valid until the request ends."""
+        t = C.c_int64()
+        rc = self.lib.ns3d_server_submit_resident(self.h, C.byref(params), C.c_void_p(int(raw_ptr)), int(dims[0]),
+                                                  int(dims[1]), int(dims[2]), int(bool(keep_fields)), C.byref(t))
         if rc != 0:
             raise NS3DError(rc, "submit failed")
         return t.value

@@ -147,9 +147,16 @@ constexpr int LOOP_GROUPS = LOOP_THREADS / LANES;
 constexpr int LOOP_MIN_BLOCKS = LOOP_THREADS >= 1024 ? 1 : 1024 / LOOP_THREADS;
 static_assert(LOOP_GROUPS >= KMAX, "the FP32 loop kernel: group s combines the partials of system s");
 struct GridBar {  // arrival counter and error flag on separate 128-byte lines
-    unsigned int count, pad0_[31];
+    unsigned int count;
+    // Zero in normal launches.  A test (ns3d_debug_barrier_timeout) sets
+    // `bias`, arrivals every barrier waits for beyond the grid's own, which
+    // never come, and `limit_ns`, a short wait limit (0 = kBarrierLimitNs).
+    unsigned int bias;
+    unsigned long long limit_ns;
+    unsigned int pad0_[28];
     int err, pad1_[31];
 };
+static_assert(sizeof(GridBar) == 256, "GridBar: two 128-byte lines");
 // per-phase time of the loop kernel (block 0, ns of the global timer)
 struct LoopProf {
     unsigned long long ns[5];

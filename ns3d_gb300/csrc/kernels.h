@@ -105,5 +105,9 @@ int device_sm_count();
 // kernels launched by this library since it was loaded
 int64_t launch_count();
 void count_launches(int64_t n);
+// zero a loop kernel's grid barrier before a launch (and apply the barrier
+// test of ns3d_debug_barrier_timeout while it is set)
+cudaError_t reset_grid_bar(GridBar *bar, cudaStream_t st);
+void set_barrier_test(unsigned int bias, unsigned long long limit_ns);
 
 }  // namespace ns3d

@@ -27,6 +27,7 @@
 // system) combines the partials, so they wait on no other block.
 #include <atomic>
 #include <cfloat>
+#include <cstring>
 
 #include "device.cuh"
 #include "kernels.h"
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     const int gstride = gridDim.x * LOOP_GROUPS;
     const int cbegin = blockIdx.x + gridDim.x * gi;
     if (threadIdx.x < A.nsys) sst[threadIdx.x] = *A.sys[threadIdx.x].st;
-    unsigned int target = 0;  // the counter is zeroed before every launch
+    unsigned int target = grid_sync_start(bar);  // the counter is zeroed before every launch
     __syncthreads();           // the scalar copies in sst are complete
     // phase times of block 0 (thread 0), kept in shared memory
     __shared__ unsigned long long s_tp[6];
@@ -520,6 +521,30 @@ __global__ void __launch_bounds__(LANES) k_spmv(SysView A, const double *__restr
     }
 }
 
+// Test hook of the bounded grid barrier (ns3d_debug_barrier_timeout): while
+// set, every loop-kernel launch's barrier waits for g_bar_bias arrivals that
+// never come, for at most g_bar_limit_ns, then the launch ends with its
+// error flag set.
+static std::atomic<unsigned int> g_bar_bias{0};
+static std::atomic<unsigned long long> g_bar_limit_ns{0};
+
+void set_barrier_test(unsigned int bias, unsigned long long limit_ns) {
+    g_bar_limit_ns = limit_ns;
+    g_bar_bias = bias;
+}
+
+cudaError_t reset_grid_bar(GridBar *bar, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
+    const unsigned int bias = g_bar_bias.load();
+    if (e != cudaSuccess || bias == 0) return e;
+    GridBar h;
+    std::memset(&h, 0, sizeof h);
+    h.bias = bias;
+    h.limit_ns = g_bar_limit_ns.load();
+    // pageable source: the copy is staged before the call returns
+    return cudaMemcpyAsync(bar, &h, sizeof h, cudaMemcpyHostToDevice, st);
+}
+
 static std::atomic<int64_t> g_launches{0};
 int64_t launch_count() { return g_launches.load(); }
 void count_launches(int64_t n) { g_launches += n; }
@@ -592,7 +617,7 @@ cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *p
         loop_occ = occ;
     }
     const int grid = krylov_loop_grid<CAP>(A.total_chunks, occ, share);
-    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
+    cudaError_t e = reset_grid_bar(bar, st);
     if (e != cudaSuccess) return e;
     KSetArgT<CAP> a = A;
     void *args[] = {&a, &bar, &prof, &max_iters};

@@ -42,9 +42,10 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, in
         red_release_add(&bar->count, 1u);
         if ((int)(ld_acquire(&bar->count) - target) < 0) {
             const unsigned long long t0 = global_ns();
+            const unsigned long long lim = bar->limit_ns ? bar->limit_ns : kBarrierLimitNs;
             unsigned int polls = 0;
             while ((int)(ld_acquire(&bar->count) - target) < 0) {
-                if ((++polls & 255u) == 0 && (global_ns() - t0 > kBarrierLimitNs || polls > 0x7fffffffu)) {
+                if ((++polls & 255u) == 0 && (global_ns() - t0 > lim || polls > 0x7fffffffu)) {
                     atomicExch(&bar->err, 1);
                     ok = 0;
                     break;
@@ -55,6 +56,12 @@ __device__ __forceinline__ bool grid_sync(GridBar *bar, unsigned int &target, in
     }
     __syncthreads();
     return *s_ok != 0;
+}
+
+// The arrival target a launch starts from (thread 0 keeps it): 0, or the
+// test bias of GridBar.
+__device__ __forceinline__ unsigned int grid_sync_start(const GridBar *bar) {
+    return threadIdx.x == 0 ? bar->bias : 0u;
 }
 
 }  // namespace ns3d

@@ -547,7 +547,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
         sst[threadIdx.x] = *A.sys[threadIdx.x].st;
         sdc[threadIdx.x] = A.sys[threadIdx.x].dc->done;
     }
-    unsigned int target = 0;
+    unsigned int target = grid_sync_start(bar);
     __syncthreads();
     int it = 0;
     for (; it < max_iters; ++it) {
@@ -997,7 +997,7 @@ cudaError_t launch_m32_loop(const MSetArgT<CAP> &A, GridBar *bar, int max_iters,
     const int grid = CAP > KMAX
                          ? std::max(1, std::min(A.total_chunks * MSUB, device_sm_count() * occ / std::max(share, 1)))
                          : loop_grid(A.total_chunks * MSUB, MSUB, occ);
-    cudaError_t e = cudaMemsetAsync(bar, 0, sizeof(GridBar), st);
+    cudaError_t e = reset_grid_bar(bar, st);
     if (e != cudaSuccess) return e;
     MSetArgT<CAP> a = A;
     void *args[] = {&a, &bar, &max_iters};

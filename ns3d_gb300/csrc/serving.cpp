@@ -50,6 +50,7 @@ struct Job {
     int64_t ticket = 0;
     ns3d_params params;
     std::vector<uint8_t> raw;
+    const uint8_t *ext = nullptr;  // caller-owned image (ns3d_server_submit_resident), not copied
     int nx = 0, ny = 0, nz = 0;
     size_t bytes = 0;
     int state = 0;  // 0 queued, 1 running, 2 done, 3 failed
@@ -63,7 +64,7 @@ struct Job {
 
 int run_one(Job &j, ns3d_group *group) {
     ns3d_handle *h = nullptr;
-    int rc = ns3d_open(&j.params, j.raw.data(), j.nx, j.ny, j.nz, &h);
+    int rc = ns3d_open(&j.params, j.ext ? j.ext : j.raw.data(), j.nx, j.ny, j.nz, &h);
     if (rc != NS3D_OK) return rc;
     if (group) rc = ns3d_set_group(h, group);
     if (rc == NS3D_OK) rc = ns3d_solve(h);
@@ -199,12 +200,13 @@ NS3D_API int ns3d_server_start(int32_t max_active, size_t hbm_budget_bytes, ns3d
     return NS3D_OK;
 }
 
-NS3D_API int ns3d_server_submit(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx, int32_t ny,
-                                int32_t nz, int32_t keep_fields, int64_t *ticket) {
+static int submit(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx, int32_t ny, int32_t nz,
+                  int32_t keep_fields, int64_t *ticket, bool copy) {
     if (!s || !p || !raw || !ticket || nx <= 0 || ny <= 0 || nz <= 0) return NS3D_ERR_ARG;
     std::unique_ptr<Job> j(new Job());
     j->params = *p;
-    j->raw.assign(raw, raw + (size_t)nx * ny * nz);
+    if (copy) j->raw.assign(raw, raw + (size_t)nx * ny * nz);
+    else j->ext = raw;
     j->nx = nx;
     j->ny = ny;
     j->nz = nz;
@@ -224,6 +226,16 @@ NS3D_API int ns3d_server_submit(ns3d_server *s, const ns3d_params *p, const uint
     s->jobs[j->ticket] = std::move(j);
     s->cv.notify_all();
     return NS3D_OK;
+}
+
+NS3D_API int ns3d_server_submit(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx, int32_t ny,
+                                int32_t nz, int32_t keep_fields, int64_t *ticket) {
+    return submit(s, p, raw, nx, ny, nz, keep_fields, ticket, true);
+}
+
+NS3D_API int ns3d_server_submit_resident(ns3d_server *s, const ns3d_params *p, const uint8_t *raw, int32_t nx,
+                                         int32_t ny, int32_t nz, int32_t keep_fields, int64_t *ticket) {
+    return submit(s, p, raw, nx, ny, nz, keep_fields, ticket, false);
 }
 
 /* state: 0 queued, 1 running, 2 done, 3 failed */

@@ -267,7 +267,8 @@ void ns3d_handle::build(const uint8_t *raw, int rx, int ry, int rz) {
     if (NU > 0x7fffffffL) throw ApiError(NS3D_ERR_ARG, "image too large for int32 indices");
     DBuf<uint8_t> draw;
     draw.alloc((size_t)rx * ry * rz, stream);
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(draw.p, raw, draw.n, cudaMemcpyHostToDevice, stream));
+    // host or device memory: the unified address space tells which
+    NS3D_CUDA_CHECK(cudaMemcpyAsync(draw.p, raw, draw.n, cudaMemcpyDefault, stream));
     img.alloc(N, stream);
     launch_build_image(draw.p, rx, ry, rz, prm.direction, std::max(prm.border, 0), prm.porevalue, img.p, nx, ny, nz,
                        stream);
@@ -836,7 +837,24 @@ static ns3d_handle *checked(ns3d_handle *h) {
     return h;
 }
 
+// A NaN or an infinity in a host input would spread through every field of
+// the solve (the reference accepts them); they are rejected at the boundary.
+static void check_finite(const char *what, const double *x, size_t n) {
+    for (size_t i = 0; i < n; ++i)
+        if (!std::isfinite(x[i]))
+            throw ApiError(NS3D_ERR_ARG, std::string(what) + ": value " + std::to_string(i) + " is not finite");
+}
+
 static void validate(const ns3d_params &p) {
+    const struct {
+        const char *name;
+        double v;
+    } reals[] = {{"dx", p.dx}, {"dy", p.dy}, {"dz", p.dz}, {"mu", p.mu}, {"rho", p.rho}, {"p0", p.p0},
+                 {"gradp", p.gradp}, {"alpha", p.alpha}, {"beta", p.beta}, {"vsolvertol", p.vsolvertol},
+                 {"psolvertol", p.psolvertol}, {"pcsolvertol", p.pcsolvertol}, {"simpletol", p.simpletol},
+                 {"deltaRMR", p.deltaRMR}};
+    for (const auto &r : reals)
+        if (!std::isfinite(r.v)) throw ApiError(NS3D_ERR_ARG, std::string("parameter ") + r.name + " is not finite");
     if (p.dx <= 0 || p.mu <= 0 || p.rho <= 0) throw ApiError(NS3D_ERR_ARG, "dx, mu and rho must be > 0");
     if (p.maxitsolver <= 0 || p.maxitSIMPLE <= 0 || p.save_step <= 0)
         throw ApiError(NS3D_ERR_ARG, "maxitsolver, maxitSIMPLE and save_step must be > 0");
@@ -849,6 +867,13 @@ static void validate(const ns3d_params &p) {
 }
 
 extern "C" {
+
+NS3D_API int ns3d_debug_barrier_timeout(int32_t extra_arrivals, double limit_s) {
+    if (extra_arrivals < 0 || (extra_arrivals > 0 && !(limit_s > 0 && limit_s <= 10)))
+        return set_error(NS3D_ERR_ARG, "ns3d_debug_barrier_timeout: extra_arrivals >= 0, 0 < limit_s <= 10");
+    set_barrier_test((unsigned)extra_arrivals, extra_arrivals ? (unsigned long long)(limit_s * 1e9) : 0ull);
+    return NS3D_OK;
+}
 
 NS3D_API int ns3d_abi_version(void) { return NS3D_ABI_VERSION; }
 NS3D_API const char *ns3d_backend_name(void) { return "gb300"; }
@@ -922,8 +947,12 @@ NS3D_API int ns3d_set_initial_fields(ns3d_handle *H, const double *pimg, const d
                                      const double *wimg) {
     NS3D_TRY
     ns3d_handle &h = *checked(H);
-    h.default_fields();
     const long N = (long)h.nx * h.ny * h.nz, NU = (long)(h.nx + 1) * h.ny * h.nz;
+    if (pimg) check_finite("initial pressure field", pimg, (size_t)N);
+    if (uimg) check_finite("initial x velocity field", uimg, (size_t)NU);
+    if (vimg) check_finite("initial y velocity field", vimg, (size_t)N);
+    if (wimg) check_finite("initial z velocity field", wimg, (size_t)N);
+    h.default_fields();
     DBuf<double> tmp;
     tmp.alloc((size_t)NU, h.stream);
     auto put = [&](const double *src, const int *map, long cells, double *f) {
@@ -956,6 +985,10 @@ NS3D_API int ns3d_get_fields(ns3d_handle *H, double *p, double *u, double *v, do
 NS3D_API int ns3d_set_fields(ns3d_handle *H, const double *p, const double *u, const double *v, const double *w) {
     NS3D_TRY
     ns3d_handle &h = *checked(H);
+    if (p) check_finite("pressure field", p, (size_t)h.np);
+    if (u) check_finite("x velocity field", u, (size_t)h.nu);
+    if (v) check_finite("y velocity field", v, (size_t)h.nv);
+    if (w) check_finite("z velocity field", w, (size_t)h.nw);
     if (p) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.p.p, p, (size_t)h.np * 8, cudaMemcpyHostToDevice, h.stream));
     if (u) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.u.p, u, (size_t)h.nu * 8, cudaMemcpyHostToDevice, h.stream));
     if (v) NS3D_CUDA_CHECK(cudaMemcpyAsync(h.v.p, v, (size_t)h.nv * 8, cudaMemcpyHostToDevice, h.stream));
@@ -1241,6 +1274,8 @@ NS3D_API int ns3d_close(ns3d_handle *h) {
 }
 
 static int64_t g_launch_base = 0;
+
+NS3D_API int64_t ns3d_kernel_launches(void) { return launch_count(); }
 
 NS3D_API int ns3d_set_profiling(ns3d_handle *H, int32_t enable) {
     NS3D_TRY

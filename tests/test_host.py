@@ -1,5 +1,6 @@
 """Host-side boundary: ini parsing (ReadInput semantics), .vti codec and the
 C-ABI symbol table of both libraries.  No GPU needed."""
+import ctypes
 import os
 import re
 
@@ -47,7 +48,8 @@ def test_oracle_exports_the_solver_symbols(oracle):
                  "ns3d_server_cancel_queued", "ns3d_solve_sweep", "ns3d_group_create", "ns3d_set_group",
                  "ns3d_group_get_stats", "ns3d_group_destroy", "ns3d_server_set_merging",
                  "ns3d_server_group_stats", "ns3d_batch_solve_merged", "ns3d_autotune_enable",
-                 "ns3d_autotune_table", "ns3d_solve_lockstep", "ns3d_batch_solve_lockstep"}
+                 "ns3d_autotune_table", "ns3d_solve_lockstep", "ns3d_batch_solve_lockstep",
+                 "ns3d_debug_barrier_timeout", "ns3d_server_submit_resident", "ns3d_kernel_launches"}
     for s in declared_symbols():
         if s not in host_only:
             assert hasattr(oracle, s), s
@@ -220,3 +222,29 @@ def test_lockstep_and_group_arguments_checked_without_work(gpulib):
     assert lib.ns3d_group_create(1, None) == capi.ERR_ARG
     assert lib.ns3d_group_get_stats(None, None) == capi.ERR_ARG
     assert lib.ns3d_set_group(None, None) == capi.ERR_ARG
+
+
+def test_non_finite_parameters_rejected_before_device_work(gpulib):
+    """A NaN or an infinity in ns3d_params is refused by ns3d_open with
+    NS3D_ERR_ARG before any device call (this runs without a GPU)."""
+    raw = np.zeros(6 * 5 * 4, np.uint8)
+    for name in ("dx", "dy", "mu", "rho", "p0", "gradp", "alpha", "beta", "pcsolvertol", "simpletol"):
+        for bad in (float("nan"), float("inf"), -float("inf")):
+            p = capi.default_params(gpulib, **{name: bad})
+            h = ctypes.c_void_p()
+            rc = gpulib.ns3d_open(ctypes.byref(p), raw.ctypes.data_as(ctypes.POINTER(ctypes.c_uint8)), 6, 5, 4,
+                                  ctypes.byref(h))
+            assert rc == capi.ERR_ARG, (name, bad)
+            assert b"not finite" in gpulib.ns3d_last_error(), name
+            assert not h.value
+
+
+def test_barrier_test_hook_arguments(gpulib):
+    f = gpulib.ns3d_debug_barrier_timeout
+    f.restype = ctypes.c_int
+    f.argtypes = [ctypes.c_int32, ctypes.c_double]
+    assert f(-1, 1.0) == capi.ERR_ARG
+    assert f(1, 0.0) == capi.ERR_ARG
+    assert f(1, 11.0) == capi.ERR_ARG
+    assert f(1, float("nan")) == capi.ERR_ARG
+    assert f(0, 0.0) == 0
