@@ -57,12 +57,15 @@ __device__ __forceinline__ void st4(double *p, const Row4 &r) {
 // not wait on each other; only the fused multiply-adds are predicated.  The
 // two rare orders (W directly before the row, E directly after it) are taken
 // only by warps that contain such a row.
-__device__ __forceinline__ double spmv_row(const KSys &S, int row, const double *__restrict__ x) {
+// The neighbour columns come from `nb` (nb[k * stride], k = slot - 1): the
+// system's table in global memory, or a chunk's copy in shared memory.
+template <class Stride>
+__device__ __forceinline__ double spmv_row_nb(const KSys &S, int row, const double *__restrict__ x, const int *nb,
+                                              Stride stride) {
     const size_t np = (size_t)S.npad;
-    const int *nb = S.nbr + row;
     const double *cf = S.coef + row;
-    const int nW = nb[0 * np], nE = nb[1 * np], nS = nb[2 * np], nN = nb[3 * np], nB = nb[4 * np],
-              nT = nb[5 * np];
+    const int nW = nb[0 * stride], nE = nb[1 * stride], nS = nb[2 * stride], nN = nb[3 * stride],
+              nB = nb[4 * stride], nT = nb[5 * stride];
     const double xP = x[row];
     const double xW = x[nW >= 0 ? nW : row], xE = x[nE >= 0 ? nE : row], xS = x[nS >= 0 ? nS : row];
     const double xN = x[nN >= 0 ? nN : row], xB = x[nB >= 0 ? nB : row], xT = x[nT >= 0 ? nT : row];
@@ -91,6 +94,10 @@ __device__ __forceinline__ double spmv_row(const KSys &S, int row, const double 
         if (nE >= 0) acc = __fma_rn(cE, xE, acc);
     }
     return acc;
+}
+
+__device__ __forceinline__ double spmv_row(const KSys &S, int row, const double *__restrict__ x) {
+    return spmv_row_nb(S, row, x, S.nbr + row, (size_t)S.npad);
 }
 
 // y = A x for the thread's rows (rows >= n give garbage that callers mask)
@@ -261,6 +268,20 @@ __global__ void k_kr_init2(const __grid_constant__ KSetArgT<CAP> A) {
 #endif
 constexpr int kSpmvUnroll = NS3D_SPMV_UNROLL;
 
+// Resident neighbour tables.  The matrix does not change during a solve, and
+// every group of the loop kernel processes the same chunks in every
+// iteration, so each group copies the six neighbour-column slabs of its
+// first chunk (6 x 1024 int32 = 24 KB) into shared memory once per launch
+// and both SpMV phases of every iteration gather through that copy: 48 B
+// per row-iteration less memory traffic, and the gathers of x no longer wait
+// for an index load from memory.  A group that owns more chunks (systems
+// above grid x LOOP_GROUPS chunks) reads the others' tables from memory.
+#ifndef NS3D_NBR_SMEM
+#define NS3D_NBR_SMEM 1
+#endif
+constexpr bool kNbrSmem = NS3D_NBR_SMEM != 0;
+constexpr size_t kNbrSmemBytes = kNbrSmem ? (size_t)LOOP_GROUPS * 6 * CH * sizeof(int) : 0;
+
 __device__ __forceinline__ bool state_active(const KState &k) { return (k.done | k.paused) == 0; }
 
 template <int CAP>
@@ -270,6 +291,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     __shared__ KState sst[CAP];
     __shared__ double sm[LOOP_GROUPS][LANES];
     __shared__ int s_ok;
+    extern __shared__ int s_nbr_all[];  // [LOOP_GROUPS][6][CH] when kNbrSmem
     const int gi = threadIdx.x / LANES, lane = threadIdx.x % LANES;
     const GroupSync gsync{gi + 1};
     // chunk c belongs to block c % gridDim.x (group (c / gridDim.x) % LOOP_GROUPS):
@@ -277,6 +299,15 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
     const int gstride = gridDim.x * LOOP_GROUPS;
     const int cbegin = blockIdx.x + gridDim.x * gi;
     if (threadIdx.x < A.nsys) sst[threadIdx.x] = *A.sys[threadIdx.x].st;
+    if (kNbrSmem && cbegin < A.total_chunks) {  // this group's first chunk, for the whole launch
+        int *const s_nbr = s_nbr_all + (size_t)gi * 6 * CH;
+        const KSys &S = A.sys[sys_of_chunk(A, cbegin)];
+        const int *src = S.nbr + (size_t)(cbegin - S.chunk_begin) * CH;
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+            for (int m = 0; m < RPL; ++m) s_nbr[k * CH + lane + m * LANES] = src[(size_t)k * S.npad + lane + m * LANES];
+    }
     unsigned int target = grid_sync_start(bar);  // the counter is zeroed before every launch
     __syncthreads();           // the scalar copies in sst are complete
     // phase times of block 0 (thread 0), kept in shared memory
@@ -321,12 +352,24 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             const int lc = c - S.chunk_begin;
             const int r0 = lc * CH + lane;
             double a = 0.0;
+            if (kNbrSmem && c == cbegin) {
+                // the resident copy: s_nbr_all[(gi * 6 + k) * CH + lane + m * LANES] for slot k, written
+                // from threadIdx.x = gi * LANES + lane so the offset stays one register
 #pragma unroll kSpmvUnroll
-            for (int m = 0; m < RPL; ++m) {
-                const int row = r0 + m * LANES;
-                const double v = spmv_row(S, row, S.y);
-                S.v[row] = v;
-                if (row < S.n) a = __fma_rn(S.r0[row], v, a);
+                for (int m = 0; m < RPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const double v = spmv_row_nb(S, row, S.y, s_nbr_all + threadIdx.x + (gi * (6 * RPL - 1) + m) * LANES, CH);
+                    S.v[row] = v;
+                    if (row < S.n) a = __fma_rn(S.r0[row], v, a);
+                }
+            } else {
+#pragma unroll kSpmvUnroll
+                for (int m = 0; m < RPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const double v = spmv_row(S, row, S.y);
+                    S.v[row] = v;
+                    if (row < S.n) a = __fma_rn(S.r0[row], v, a);
+                }
             }
             const double t = lanes_tree_sum(a, lane, sm[gi], gsync);
             if (lane == 0) S.part[4 * (size_t)S.nchunks + lc] = t;
@@ -365,14 +408,27 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
             const int lc = c - S.chunk_begin;
             const int r0 = lc * CH + lane;
             double att = 0.0, ats = 0.0;
+            if (kNbrSmem && c == cbegin) {
 #pragma unroll kSpmvUnroll
-            for (int m = 0; m < RPL; ++m) {
-                const int row = r0 + m * LANES;
-                const double t = spmv_row(S, row, S.z);
-                S.t[row] = t;
-                if (row < S.n) {
-                    att = __fma_rn(t, t, att);
-                    ats = __fma_rn(t, S.s[row], ats);
+                for (int m = 0; m < RPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const double t = spmv_row_nb(S, row, S.z, s_nbr_all + threadIdx.x + (gi * (6 * RPL - 1) + m) * LANES, CH);
+                    S.t[row] = t;
+                    if (row < S.n) {
+                        att = __fma_rn(t, t, att);
+                        ats = __fma_rn(t, S.s[row], ats);
+                    }
+                }
+            } else {
+#pragma unroll kSpmvUnroll
+                for (int m = 0; m < RPL; ++m) {
+                    const int row = r0 + m * LANES;
+                    const double t = spmv_row(S, row, S.z);
+                    S.t[row] = t;
+                    if (row < S.n) {
+                        att = __fma_rn(t, t, att);
+                        ats = __fma_rn(t, S.s[row], ats);
+                    }
                 }
             }
             double tt, ts;
@@ -611,7 +667,12 @@ cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *p
     static std::atomic<int> loop_occ{0};
     int occ = loop_occ.load();
     if (occ == 0) {
-        cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kr_loop<CAP>, LOOP_THREADS, 0);
+        cudaError_t e = cudaSuccess;
+        if (kNbrSmemBytes > 0)
+            e = cudaFuncSetAttribute((const void *)k_kr_loop<CAP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)kNbrSmemBytes);
+        if (e != cudaSuccess) return e;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_kr_loop<CAP>, LOOP_THREADS, kNbrSmemBytes);
         if (e != cudaSuccess) return e;
         if (occ <= 0) return cudaErrorLaunchOutOfResources;
         loop_occ = occ;
@@ -622,7 +683,7 @@ cudaError_t launch_krylov_loop(const KSetArgT<CAP> &A, GridBar *bar, LoopProf *p
     KSetArgT<CAP> a = A;
     void *args[] = {&a, &bar, &prof, &max_iters};
     count_launches(1);
-    return cudaLaunchCooperativeKernel((const void *)k_kr_loop<CAP>, grid, LOOP_THREADS, args, 0, st);
+    return cudaLaunchCooperativeKernel((const void *)k_kr_loop<CAP>, grid, LOOP_THREADS, args, kNbrSmemBytes, st);
 }
 
 template <int CAP>
