@@ -168,7 +168,11 @@ void KrylovSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st,
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_st_.p, st_.p, ns * sizeof(KState), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaMemcpyAsync(h_err_.p, &bar_.p->err, sizeof(int), cudaMemcpyDeviceToHost, st));
         NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
-        if (h_err_.p[0]) throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel: a grid barrier timed out");
+        // the flag belongs to this run's last loop launch (before the first
+        // one it still holds the previous run's: a timed-out solve must not
+        // poison the next)
+        if (loops > 0 && h_err_.p[0])
+            throw ApiError(NS3D_ERR_TIMEOUT, "BiCGSTAB loop kernel: a grid barrier timed out");
         bool all_done = true, any_paused = false;
         int progress = 0;
         int64_t rows = 0;
