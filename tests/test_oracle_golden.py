@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from helpers import golden, solver, spheres_params
-from ns3d_gb300 import synth
+from ns3d_gb300 import capi, synth
 
 LATTICES = {"spheres_64.vti": (64, 8, 3), "spheres_128.vti": (128, 12, 5)}
 
@@ -65,9 +65,11 @@ def test_readme_64_table(oracle, method):
     """README.md 64^3 compare_algorithms table: K within 1e-4 relative and the
     same outer-iteration counts for SIMPLEC, SIMPLERR and IDEAL.  SIMPLER's
     RMR sits on a noisy plateau near simpletol = 1e-4, where any change of
-    rounding moves the crossing (42 iterations in the README); for it the bar
-    is the README's own cross-algorithm agreement, K within 0.1 %
-    (README.md:190-192)."""
+    rounding moves the crossing: the oracle under three roundings of its
+    BiCGSTAB arithmetic converges in 25 and 26 iterations or not within 200
+    (oracle/rounding_experiment.json; the README has 42), with K spread by
+    3.5e-4.  For it the bar is the README's own cross-algorithm agreement, K
+    within 0.1 % (README.md:190-192)."""
     img = synth.sphere_lattice(64, 8, 3)
     s = solver(oracle, img, spheres_params(oracle, maxitSIMPLE=200, method=method))
     r = s.solve()
@@ -79,3 +81,78 @@ def test_readme_64_table(oracle, method):
         assert r.iterations == t["iterations"]
     else:
         assert abs(r.K - t["K"]) / t["K"] < 1e-3
+
+
+# ---- the whole golden run ---------------------------------------------------
+# tests/golden/make_golden_run.py ran the oracle on the reference's golden case
+# (tests/test_spheres.ini, 128^3 lattice, SIMPLEC, 30 outer iterations) and
+# committed its logs; the GPU path reproduces those logs bit for bit
+# (tests/test_gpu_fixtures.py).  Here they are held against the reference's own
+# outputs.  The pressure-correction solves stop at pcsolvertol = 1e-3, so any
+# change of rounding moves their Krylov path.  Three roundings of the
+# oracle's own arithmetic (oracle/rounding_experiment.py, results in
+# oracle/rounding_experiment.json) spread the K of an iteration by up to
+# 3.3e-3 (2.6e-4 over iterations 20-29); a 4-wide SIMD-style dot-product
+# rounding even meets the reference's iteration-1 K to 5e-15.  Measured
+# against the reference: K and the flow columns within 1.9e-3 (the largest at
+# iterations 2-4, where the relaxation is still moving), within 1.7e-4 over
+# the last ten iterations -- inside the spread rounding alone produces --, the
+# velocity-field norm within 4e-5, and every momentum solve's iteration count
+# equal.
+
+GOLDEN_RUN_FLOW_TOL = 2.5e-3   # Q, <u_out>, RMR, K, Lref*maxdiv/<u_out>, maxdiv: all 30 rows
+GOLDEN_RUN_LATE_TOL = 3e-4     # K over iterations 20-29
+GOLDEN_RUN_NORM_TOL = 5e-4     # ||Div_u||
+GOLDEN_RUN_UNORM_TOL = 1e-4    # <||u||>
+GOLDEN_FIELD_TOL = {"P": 1e-10, "Vx": 1e-4, "Vy": 3e-4, "Vz": 3e-4}
+
+
+def _oracle_golden_log(kind):
+    import gzip
+    import os
+    path = os.path.join(os.path.dirname(__file__), "golden", "oracle_logs", "lattice128_golden.%s.gz" % kind)
+    with gzip.open(path, "rt") as f:
+        return f.read().splitlines()
+
+
+def test_whole_golden_run_res_rows():
+    """All 30 RES rows of the golden run, every column."""
+    g = golden()
+    mine = [[x.strip() for x in l.split(",")] for l in _oracle_golden_log("RES")[1:]]
+    assert len(mine) == len(g["res_rows"]) == 30
+    for row, gold in zip(mine, g["res_rows"]):
+        assert int(row[0]) == gold[0]
+        it = gold[0]
+        for k in (1, 2, 3, 4, 7, 9):  # Q, <u_out>, RMR, K, Lref*maxdiv/<u_out>, maxdiv
+            assert float(row[k]) == pytest.approx(gold[k], rel=GOLDEN_RUN_FLOW_TOL), (it, k)
+        assert float(row[5]) == pytest.approx(gold[5], rel=1e-6)  # gradP
+        assert float(row[6]) == pytest.approx(gold[6], rel=GOLDEN_RUN_NORM_TOL), it
+        assert float(row[8]) == pytest.approx(gold[8], rel=GOLDEN_RUN_UNORM_TOL), it
+        assert [int(x) for x in row[10:13]] == gold[10:13], it  # momentum solves: identical counts
+        # it_pc, the last pressure-correction solve's count, follows the Krylov
+        # path that rounding moves (tolerance 1e-3); it is not compared
+
+
+def test_whole_golden_run_k_lines():
+    """The 15-digit K of every outer iteration (INFO log)."""
+    g = golden()
+    mine = [float(l.split(":")[1]) for l in _oracle_golden_log("INFO") if l.startswith("Permeability K")]
+    gold = [float(x) for x in g["info_K_per_iteration"]]
+    assert len(mine) == len(gold) == 30
+    assert abs(mine[0] - gold[0]) <= 1e-12 * gold[0]
+    for it, (a, b) in enumerate(zip(mine, gold)):
+        assert abs(a - b) <= GOLDEN_RUN_FLOW_TOL * b, it
+        if it >= 20:
+            assert abs(a - b) <= GOLDEN_RUN_LATE_TOL * b, it
+
+
+def test_golden_fields_relative_l2():
+    """The oracle's fields at iterations 20 (the -SAVE-1 snapshot) and 30
+    against the reference's golden .vti fields, relative L2 over the image
+    (measured by make_golden_run.py, which reads the reference's files)."""
+    import json
+    import os
+    rec = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "oracle_lattice128_golden.json")))
+    for snap in ("iteration_20", "iteration_30"):
+        for name, tol in GOLDEN_FIELD_TOL.items():
+            assert rec["field_rel_l2_vs_golden"][snap][name]["rel_l2"] <= tol, (snap, name)
