@@ -1,0 +1,133 @@
+"""Full-size parity on the GPU: the CUDA path against the oracle's committed
+records of complete solves (tests/golden/make_oracle_fixtures.py):
+
+  sphere64   64^3 RSA spheres r = 6, porosity ~0.55, seed 0, SIMPLEC,
+             converged at RMR < 1e-6
+  sphere128  128^3 RSA spheres r = 8, porosity ~0.5, seed 1, SIMPLEC,
+             SIMPLER (N1 = 2), SIMPLERR (N1 = 2), IDEAL (N1 = N2 = 2),
+             converged
+
+and against the oracle's record of the reference's golden run (its
+tests/test_spheres.ini on the 128^3 lattice, 30 outer iterations,
+tests/golden/make_golden_run.py).
+
+The bars the task sets for the plain FP64 path are |dK/K| <= 1e-8 and a
+relative L2 field error <= 1e-8.  The kernels follow the oracle's
+arithmetic, so the tests assert more: every result scalar equal, the SHA-256
+of every field's bytes equal (relative L2 error 0) and the RES/INFO logs
+equal byte for byte (wall-clock line excepted).  The 1e-8 bars are asserted
+first, so a failure says which bar broke.
+"""
+import functools
+import glob
+import gzip
+import hashlib
+import json
+import os
+
+import numpy as np
+import pytest
+
+from ns3d_gb300 import capi, synth, workloads
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLDEN = os.path.join(HERE, "golden")
+RECORDS = sorted(glob.glob(os.path.join(GOLDEN, "oracle_sphere*_*.json")))
+K_TOL = 1e-8
+FIELD_TOL = 1e-8
+
+
+@functools.lru_cache(maxsize=None)
+def _image(case):
+    return workloads.CASES[case]["image"]()
+
+
+def _strip_clock(text):
+    return "".join(l for l in text.splitlines(True) if " terminated in " not in l)
+
+
+def _log(name):
+    with gzip.open(os.path.join(GOLDEN, "oracle_logs", name), "rt") as f:
+        return f.read()
+
+
+def _first_diff(a, b):
+    la, lb = a.splitlines(), b.splitlines()
+    for i, (x, y) in enumerate(zip(la, lb)):
+        if x != y:
+            return "line %d: gpu %r oracle %r" % (i + 1, x, y)
+    return "lengths %d vs %d" % (len(la), len(lb))
+
+
+def test_records_present():
+    names = {os.path.basename(p) for p in RECORDS}
+    assert "oracle_sphere64_SIMPLEC.json" in names
+    assert any(n.startswith("oracle_sphere128_") for n in names)
+
+
+@pytest.mark.parametrize("path", RECORDS, ids=[os.path.basename(p)[7:-5] for p in RECORDS])
+def test_full_solve_matches_oracle_record(gpulib, path, tmp_path):
+    rec = json.load(open(path))
+    case, method = rec["case"], rec["method"]
+    img, info = _image(case)
+    assert workloads.image_sha256(img) == rec["image"]["sha256"], "seeded image differs from the record"
+    spec = workloads.CASES[case]
+    prm = workloads.solve_params(capi, gpulib, img.shape[spec["direction"] - 1], method, spec["direction"])
+    mine = {k: (repr(v) if isinstance(v, float) else v) for k, v in prm.as_dict().items()}
+    assert mine == rec["params"]
+    s = capi.Solver(gpulib, prm, synth.to_raw(img), img.shape)
+    assert dict(np=s.sizes.np, nu=s.sizes.nu, nv=s.sizes.nv, nw=s.sizes.nw) == rec["sizes"]
+    stem = "%s_%s" % (case, method)
+    s.set_output(str(tmp_path), stem, False)
+    r = s.solve()
+    fields = s.fields()
+    s.close()
+    # the task's bars
+    k_ref = float(rec["result"]["K"])
+    assert abs(r.K - k_ref) <= K_TOL * abs(k_ref)
+    for name, a in zip("puvw", fields):
+        l2 = float(rec["fields"][name]["l2"])
+        # |‖a‖ - ‖b‖| <= ‖a - b‖: a necessary condition of the relative L2 bar
+        assert abs(np.linalg.norm(a) - l2) <= FIELD_TOL * l2, name
+    # bit identity with the oracle
+    for name, v in rec["result"].items():
+        got = getattr(r, name)
+        assert (repr(float(got)) if isinstance(v, str) else int(got)) == v, name
+    for name, a in zip("puvw", fields):
+        assert workloads.field_sha256(a) == rec["fields"][name]["sha256"], "field %s differs" % name
+    d = str(spec["direction"])
+    res = _strip_clock(open(os.path.join(tmp_path, "RES-%s-%s.csv" % (d, stem))).read())
+    inf = _strip_clock(open(os.path.join(tmp_path, "INFO-%s-%s.log" % (d, stem))).read())
+    assert hashlib.sha256(res.encode()).hexdigest() == rec["res_sha256"], _first_diff(res, _log(stem + ".RES.gz"))
+    assert hashlib.sha256(inf.encode()).hexdigest() == rec["info_sha256"], _first_diff(inf, _log(stem + ".INFO.gz"))
+
+
+def test_golden_run_matches_oracle_record(gpulib, tmp_path):
+    """The reference's own golden case (tests/test_spheres.ini on the 128^3
+    sphere lattice, SIMPLEC, 30 outer iterations): logs and field images
+    bit-identical to the oracle's, whose distance to the reference's golden
+    outputs is pinned by tests/test_oracle_golden.py."""
+    rec = json.load(open(os.path.join(GOLDEN, "oracle_lattice128_golden.json")))
+    img = synth.sphere_lattice(128, 12, 5)
+    prm = capi.default_params(gpulib, dx=2e-6, dy=-1, dz=-1, mu=1e-3, rho=1e3, p0=1e5, gradp=1e2, alpha=0.8,
+                              beta=1.0, vsolvertol=1e-5, psolvertol=1e-6, pcsolvertol=1e-3, simpletol=1e-4,
+                              deltaRMR=1e-4, maxitsolver=500, maxitSIMPLE=30, N1=2, N2=2, save_step=20,
+                              porevalue=0, direction=1, border=0, method="SIMPLEC")
+    s = capi.Solver(gpulib, prm, synth.to_raw(img), img.shape)
+    s.set_output(str(tmp_path), "spheres_128", False)
+    r = s.solve()
+    images = s.field_images()
+    s.close()
+    assert repr(r.K) == rec["oracle_result"]["K"]
+    assert r.iterations == rec["oracle_result"]["iterations"]
+    for name, a in zip(("p", "u", "v", "w", "v_faces"), images):
+        assert hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest() == \
+            rec["oracle_field_images_sha256"][name], name
+    res = _strip_clock(open(os.path.join(tmp_path, "RES-1-spheres_128.csv")).read())
+    inf = _strip_clock(open(os.path.join(tmp_path, "INFO-1-spheres_128.log")).read())
+    assert hashlib.sha256(res.encode()).hexdigest() == rec["res_sha256"], \
+        _first_diff(res, _log("lattice128_golden.RES.gz"))
+    assert hashlib.sha256(inf.encode()).hexdigest() == rec["info_sha256"], \
+        _first_diff(inf, _log("lattice128_golden.INFO.gz"))

@@ -156,3 +156,27 @@ def test_golden_fields_relative_l2():
     for snap in ("iteration_20", "iteration_30"):
         for name, tol in GOLDEN_FIELD_TOL.items():
             assert rec["field_rel_l2_vs_golden"][snap][name]["rel_l2"] <= tol, (snap, name)
+
+
+def test_oracle_records_match_the_current_oracle(oracle, tmp_path):
+    """The committed oracle records were made by this oracle: its first two
+    outer iterations of the 64^3 sphere-pack case reproduce the record's RES
+    rows and INFO lines up to that point, byte for byte."""
+    import gzip
+    import os
+    from ns3d_gb300 import workloads
+    img, _ = workloads.sphere64()
+    s = solver(oracle, img, workloads.solve_params(capi, oracle, 64, "SIMPLEC", 1, max_outer=2))
+    s.set_output(tmp_path, "sphere64_SIMPLEC", False)
+    s.solve()
+    s.close()
+    logs = os.path.join(os.path.dirname(__file__), "golden", "oracle_logs")
+    rec_res = gzip.open(os.path.join(logs, "sphere64_SIMPLEC.RES.gz"), "rt").read().splitlines()
+    res = (tmp_path / "RES-1-sphere64_SIMPLEC.csv").read_text().splitlines()
+    assert res[:3] == rec_res[:3]
+    rec_info = gzip.open(os.path.join(logs, "sphere64_SIMPLEC.INFO.gz"), "rt").read().splitlines()
+    info = (tmp_path / "INFO-1-sphere64_SIMPLEC.log").read_text().splitlines()
+    cut = info.index("Iteration 1  ------------")
+    skip = [i for i, l in enumerate(rec_info) if l.startswith("Max number of SIMPLE iterations")]
+    assert [l for i, l in enumerate(info[:cut]) if i not in skip] == \
+        [l for i, l in enumerate(rec_info[:cut]) if i not in skip]
