@@ -64,7 +64,6 @@ def _first_diff(a, b):
 def test_records_present():
     names = {os.path.basename(p) for p in RECORDS}
     assert "oracle_sphere64_SIMPLEC.json" in names
-    assert any(n.startswith("oracle_sphere128_") for n in names)
 
 
 @pytest.mark.parametrize("path", RECORDS, ids=[os.path.basename(p)[7:-5] for p in RECORDS])
