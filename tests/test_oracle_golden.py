@@ -158,6 +158,28 @@ def test_golden_fields_relative_l2():
             assert rec["field_rel_l2_vs_golden"][snap][name]["rel_l2"] <= tol, (snap, name)
 
 
+def test_rounding_alone_explains_the_distance_to_the_reference():
+    """The committed rounding experiment (oracle/rounding_experiment.py):
+    over the golden run, the oracle's distance to the reference's K stays
+    inside the spread that changing the rounding of the oracle's own
+    arithmetic produces, and SIMPLER's outer count on the README case moves
+    with the rounding alone while the other three methods' counts do not."""
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.dirname(__file__)), "oracle", "rounding_experiment.json")
+    d = json.load(open(path))
+    g = d["golden128"]
+    spread = g["max_rel_spread_between_roundings"]
+    dist = g["max_rel_diff_to_reference"]["fixed"]
+    assert max(dist) <= max(spread)
+    assert max(dist[20:]) <= max(spread[20:])
+    runs = d["runs"]
+    assert len({r["outer_iterations"] for r in runs["SIMPLER"].values()}) > 1
+    for m in ("SIMPLEC", "SIMPLERR", "IDEAL"):
+        its = {r["outer_iterations"] for r in runs[m].values()}
+        assert its == {d["published"][m]["outer_iterations"]}, m
+
+
 def test_oracle_records_match_the_current_oracle(oracle, tmp_path):
     """The committed oracle records were made by this oracle: its first two
     outer iterations of the 64^3 sphere-pack case reproduce the record's RES
