@@ -490,14 +490,22 @@ __device__ __forceinline__ bool mg_precondition(const MSetArgT<CAP> &A, const KS
 
 // Galerkin operator of a coarse level: per row, the sum of its block's
 // diagonal and internal couplings, and per direction the couplings that
-// leave the block (in the members' order)
+// leave the block (in the members' order).
+// A block that holds a whole isolated pore cluster (no path to the inlet or
+// outlet: its rows sum to zero, the block is singular) gets a coarse
+// diagonal that cancels to a rounding residue; 1/residue would blow the
+// coarse correction up.  Such a diagonal (below kSingular of its members'
+// diagonals in magnitude) gets no coarse correction: inverse diagonal 0.
+constexpr float kSingular = 1e-4f;
+
 __global__ void k_mg_galerkin(int npad_f, const int *__restrict__ nbr_f, const float *__restrict__ coef_f,
                               MGLevel C) {
     for (int I = blockIdx.x * blockDim.x + threadIdx.x; I < C.n; I += gridDim.x * blockDim.x) {
-        float d = 0.0f, off[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+        float d = 0.0f, dabs = 0.0f, off[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
         for (int q = C.mstart[I]; q < C.mstart[I + 1]; ++q) {
             const int m = C.members[q];
             d += coef_f[m];
+            dabs += fabsf(coef_f[m]);
 #pragma unroll
             for (int dir = 0; dir < 6; ++dir) {
                 const int col = nbr_f[(size_t)dir * npad_f + m];
@@ -510,7 +518,7 @@ __global__ void k_mg_galerkin(int npad_f, const int *__restrict__ nbr_f, const f
         C.coef[I] = d;
 #pragma unroll
         for (int dir = 0; dir < 6; ++dir) C.coef[(size_t)(dir + 1) * C.npad + I] = off[dir];
-        C.invdiag[I] = d != 0.0f ? 1.0f / d : 1.0f;
+        C.invdiag[I] = fabsf(d) > kSingular * dabs ? 1.0f / d : 0.0f;
     }
 }
 
