@@ -78,12 +78,20 @@ def field_sha256(a):
 # of overlapping spheres (radius 3-8 voxels) or of isotropic straight fibres
 # (radius 2-4), porosity uniform in [0.35, 0.95], rasterised on the device
 # (ns3d_generate_image); flow along x, y or z; SIMPLEC or IDEAL.  The
-# physics is the creeping-flow setting above; the numerics are
-# STREAM_NUMERICS.
+# physics is the creeping-flow setting above.  The numerics
+# (STREAM_NUMERICS) take the outer-loop settings of the reference's own
+# benchmark input (its tests/compare_algorithms.ini: alpha 0.8, convergence
+# at RMR < 1e-4) and the linear-solver tolerances of the 64^3 case (1e-8, at
+# most 2000 iterations): with tight inner solves, the plain FP64 and the
+# mixed-precision solves of a request follow the same outer trajectory, so
+# their K agree far inside 1e-4 (with the reference's loose inner tolerances,
+# 1e-3 for the pressure correction, the two trajectories part and K differs
+# by up to 3e-3 at RMR < 1e-4); the outer tolerance keeps the large
+# high-porosity requests to hundreds of outer iterations.
 STREAM_SEED = 4
 STREAM_EDGE = (48, 192)
-STREAM_NUMERICS = dict(alpha=0.8, vsolvertol=1e-5, psolvertol=1e-6, pcsolvertol=1e-3, simpletol=1e-4,
-                       maxitsolver=500)
+STREAM_NUMERICS = dict(alpha=0.8, vsolvertol=1e-8, psolvertol=1e-8, pcsolvertol=1e-8, simpletol=1e-4,
+                       maxitsolver=2000)
 
 
 def stream_request(i, seed=STREAM_SEED):
