@@ -495,7 +495,7 @@ def run_gpu(args):
     dev = torch.device("cuda", torch.cuda.current_device())
     lib = ns3d_gb300.lib()
     W, K = args.warmup, args.steps
-    base = rank * 100000  # each replica serves its own part of the stream
+    base = args.first + rank * 100000  # each replica serves its own part of the stream
     items = [materialize(capi, lib, workloads.stream_request(base + i), torch, dev) for i in range(W + K)]
     warm, timed = items[:W], items[W:]
     # warm-up: the first W requests served, and the smallest alone on the plain path
@@ -533,7 +533,7 @@ def run_gpu(args):
         sweep = None
         if args.sweep and world == 1:
             sweep = {}
-            nxt = W + K
+            nxt = args.first + W + K
             for q, rate in enumerate(SWEEP_RATES):
                 seg = [materialize(capi, lib, workloads.stream_request(nxt + j), torch, dev)
                        for j in range(args.sweep_requests)]
@@ -633,6 +633,8 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=12, help="timed requests of the stream")
     ap.add_argument("--warmup", type=int, default=3, help="requests served before the timed legs")
+    ap.add_argument("--first", type=int, default=0,
+                    help="index of the first request of the stream used (0; profiling runs pick small ones)")
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--cpu-4-threads", action="store_true", help="add a 4-thread CPU-oracle solve (minutes)")
