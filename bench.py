@@ -75,6 +75,7 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+T_START = time.perf_counter()
 METRIC = "permeability solves/sec and p50/p99 latency at |dK/K|<=1e-4 vs plain FP64 GPU"
 MAX_OUTER = 2000
 SAT_RATE = 20.0            # arrivals per second of the timed legs (saturating)
@@ -222,6 +223,11 @@ def materialize(capi, lib, req, torch, dev):
     out = dict(req)
     out.update(achieved_porosity=ach, host=host, dev=d, nbytes=raw.nbytes)
     return out
+
+
+def note(*a):
+    """Progress on stderr (the JSON line is the only stdout output)."""
+    print("[bench %.0f s]" % (time.perf_counter() - T_START), *a, file=sys.stderr, flush=True)
 
 
 def describe(it):
@@ -498,20 +504,24 @@ def run_gpu(args):
     base = args.first + rank * 100000  # each replica serves its own part of the stream
     items = [materialize(capi, lib, workloads.stream_request(base + i), torch, dev) for i in range(W + K)]
     warm, timed = items[:W], items[W:]
+    note("stream ready: edges", [it["shape"][0] for it in items])
     # warm-up: the first W requests served, and the smallest alone on the plain path
     if warm:
         serve_leg(capi, workloads, lib, warm, SAT_RATE, 1000 + rank, torch)
         plain_leg(capi, workloads, lib, [min(warm, key=lambda it: it["shape"][0])], torch)
+    note("warm-up done")
     clocks = Clocks(local) if rank == 0 else None
     barrier(dist)
     # plain FP64, one request at a time
     t_plain, plain, prof = plain_leg(capi, workloads, lib, timed, torch)
+    note("plain FP64 leg: %.1f s" % t_plain)
     # served, images in HBM
     barrier(dist)
     elapsed, served, failed, launches, _ = serve_leg(capi, workloads, lib, timed, SAT_RATE, 2000 + rank, torch)
     barrier(dist)
     elapsed = reduce_max(dist, elapsed)
     clk = clocks.stop() if clocks else None
+    note("served leg: %.1f s" % elapsed)
     # end to end: pinned host images in, fields out
     sizes = [r["sizes"] for r in plain]
     e2e_elapsed, e2e_failed = None, None
@@ -520,6 +530,7 @@ def run_gpu(args):
         e2e_elapsed, _, e2e_failed, _, _ = serve_leg(capi, workloads, lib, timed, SAT_RATE, 2000 + rank, torch,
                                                      resident=False, keep_fields=True, sizes=sizes)
         e2e_elapsed = reduce_max(dist, e2e_elapsed)
+        note("end-to-end leg: %.1f s" % e2e_elapsed)
     value = world * K / elapsed
     plain_rate = K / t_plain
     errs = [abs(s["K"] - p["K"]) / abs(p["K"]) if (s and p["K"] != 0) else None for s, p in zip(served, plain)]
@@ -544,6 +555,7 @@ def run_gpu(args):
                                            "solves_per_s": (len(seg) - fl) / el, "p50_latency_s": a,
                                            "p99_latency_s": b, "edges": [it["shape"][0] for it in seg]}
                 del seg
+                note("sweep rate %g: %.1f s" % (rate, el))
         cpu, sphere64 = None, None
         if args.cpu_baseline and world == 1:
             sphere64 = {"gpu_plain_fp64": gpu_sphere64(capi, workloads, lib)}
@@ -554,6 +566,7 @@ def run_gpu(args):
                 sphere64["cpu_oracle_4_threads"] = oracle_complete_solve(4)
             sphere64["gpu_speedup_vs_cpu_oracle"] = o["seconds"] / sphere64["gpu_plain_fp64"]["seconds"]
             sphere64["K_rel_diff_gpu_vs_oracle"] = abs(sphere64["gpu_plain_fp64"]["K"] - o["K"]) / abs(o["K"])
+            note("cpu baseline: %.1f s on %d threads" % (o["seconds"], cores))
             cpu = {"value": 1.0 / o["seconds"], "unit": "solves/s", "cores": cores, "kind": "port",
                    "sample": "complete CPU-oracle solves of the 64^3 sphere pack (radius 6, porosity 0.55, SIMPLEC, "
                              "tolerances 1e-8, RMR < 1e-6; %d outer iterations, %.1f s) with %d OpenMP threads = "
