@@ -42,7 +42,7 @@ next `--steps K` requests are timed in every leg.
               (workloads.sphere64: radius 6, porosity 0.55, SIMPLEC,
               tolerances 1e-8, RMR < 1e-6) with every physical host core,
               beside the plain FP64 GPU solve of the same case
-  batch64     64 uneven images (edges from {32..96} per axis, sphere or fibre
+  batch64     (opt-in, --batch64) 64 uneven images (edges from {32..96} per axis, sphere or fibre
               packs, SIMPLEC, flow x) solved one at a time in plain FP64 and
               together in mixed precision on concurrent streams, as merged
               persistent launches over the ragged chunk list, and in lockstep
@@ -676,8 +676,8 @@ def main():
     ap.add_argument("--serving-active", type=int, default=SERVE_ACTIVE, help="solves in flight at most")
     ap.add_argument("--no-readme64", dest="readme64", action="store_false",
                     help="skip the reference's published 64^3 four-method case")
-    ap.add_argument("--no-batch64", dest="batch64", action="store_false",
-                    help="skip the 64-image batch sample (streams, merged sets, lockstep)")
+    ap.add_argument("--batch64", action="store_true",
+                    help="add the 64-image batch sample (streams, merged sets, lockstep; about four minutes)")
     ap.add_argument("--batch64-images", type=int, default=64)
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
     ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)
