@@ -62,10 +62,34 @@ struct ns3d_handle {
         for (size_t i = 0; i < items.size(); ++i) items[i].mg = own.uses_mg((int)i);
         group->run_mixed(items, stream, own.out_state_buffer(), out, own.variant());
     }
+    // A pressure(-correction) solve.  In the mixed modes a solve that ends
+    // without success (no convergence within the iteration cap, or a
+    // numerical breakdown of the FP32 inner solves -- on strongly fragmented
+    // pore spaces, whose many isolated clusters give singular blocks, the
+    // FP32 solves stall) is redone in plain FP64 from the guess it started
+    // from, and the rest of this solve's pressure systems go straight to
+    // FP64.  The reported outcome is the FP64 solve's; both solves' work is
+    // counted.
+    bool p_fp64 = false;  // reset by begin_solve
+    ns3d::DBuf<double> p_guess;
     void solve_p(const std::vector<ns3d::SolveItem> &items, std::vector<ns3d::SolveOutcome> &out) {
-        if (mixed()) run_mixed(mp, items, out);
-        else run_fp64(kp, items, out);
+        if (!mixed() || p_fp64) {
+            run_fp64(kp, items, out);
+            return;
+        }
+        const ns3d::DevSys &S = *items[0].sys;
+        if (p_guess.n < (size_t)S.npad) p_guess.alloc(S.npad, stream);
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(p_guess.p, items[0].x, (size_t)S.npad * 8, cudaMemcpyDeviceToDevice, stream));
+        run_mixed(mp, items, out);
+        if (out[0].info == NS3D_SUCCESS) return;
+        p_fallbacks += 1;
+        p_fp64 = true;
+        const int wasted = out[0].work;
+        NS3D_CUDA_CHECK(cudaMemcpyAsync(items[0].x, p_guess.p, (size_t)S.npad * 8, cudaMemcpyDeviceToDevice, stream));
+        run_fp64(kp, items, out);
+        out[0].work += wasted;
     }
+    int p_fallbacks = 0;  // mixed pressure solves redone in FP64 (all solves of this handle)
 
     // physical constants and relaxation state (NavierStokesBase members)
     double dx, dy, dz, mu, rho, p0, p1, gradp, alpha0, beta0, alpha, beta;

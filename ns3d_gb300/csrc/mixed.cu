@@ -945,30 +945,6 @@ __global__ void k_to_f32(const double *__restrict__ coef, const double *__restri
 // ---- launchers ------------------------------------------------------------------
 static inline int m_grid(int total_chunks) { return std::max(1, std::min(total_chunks, device_sm_count() * 32)); }
 
-// One row of each isolated pore cluster becomes an identity row of the FP32
-// copy.  The cluster's block is singular (its rows sum to zero), and FP32
-// rounding makes the right-hand side slightly inconsistent, so the FP32
-// Krylov iterates grow along the block's constant mode until the inner solve
-// breaks down.  With the row pinned the block is regular; since the block's
-// columns also sum to zero, a correction that satisfies the other rows of a
-// consistent cluster satisfies the pinned row of the original system too.
-// The FP64 residual and step of every round use the original matrix.
-__global__ void k_pin_rows(float *coef32, float *invdiag32, int npad, const int *__restrict__ pins, int npins) {
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < npins; q += gridDim.x * blockDim.x) {
-        const int r = pins[q];
-        coef32[r] = 1.0f;
-        for (int s = 1; s < 7; ++s) coef32[(size_t)s * npad + r] = 0.0f;
-        invdiag32[r] = 1.0f;
-    }
-}
-
-void launch_pin_rows(float *coef32, float *invdiag32, int npad, const int *pins, int npins, cudaStream_t st) {
-    if (npins <= 0) return;
-    count_launches(1);
-    k_pin_rows<<<std::max(1, std::min((npins + 255) / 256, 152 * 8)), 256, 0, st>>>(coef32, invdiag32, npad, pins,
-                                                                                      npins);
-}
-
 void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
                    cudaStream_t st) {
     const long total = 8L * npad;

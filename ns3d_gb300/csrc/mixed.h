@@ -75,8 +75,6 @@ static_assert(sizeof(MSetArgMerged) <= 32000, "kernel parameter space");
 
 // Galerkin operators of every coarse level of `mg` from the FP32 system
 void launch_mg_galerkin(const MSys &sys, cudaStream_t st);
-// rows `pins` of an FP32 system become identity rows (isolated clusters)
-void launch_pin_rows(float *coef32, float *invdiag32, int npad, const int *pins, int npins, cudaStream_t st);
 void launch_to_f32(const double *coef, const double *invdiag, int npad, float *coef32, float *invdiag32,
                    cudaStream_t st);
 // (the set launchers are instantiated for CAP = KMAX and KMAX_MERGED_M)

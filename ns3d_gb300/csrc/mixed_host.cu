@@ -94,48 +94,6 @@ static void build_mg(DevSys &S, cudaStream_t st) {
     S.mg = std::move(H);
 }
 
-// Rows to pin in the FP32 copy of pressure system S: the smallest row of
-// every connected component of its graph that has no cell on the inlet or
-// outlet plane (i = 0 or i = nx - 1, where the boundary terms make the rows
-// diagonally dominant).  Found once per geometry (union-find on the host).
-static void find_isolated_clusters(DevSys &S, cudaStream_t st) {
-    std::vector<int> cell((size_t)S.n), nbr((size_t)6 * S.npad);
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(cell.data(), S.cell.p, (size_t)S.n * 4, cudaMemcpyDeviceToHost, st));
-    NS3D_CUDA_CHECK(cudaMemcpyAsync(nbr.data(), S.nbr.p, nbr.size() * 4, cudaMemcpyDeviceToHost, st));
-    NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
-    std::vector<int> up((size_t)S.n);
-    for (int r = 0; r < S.n; ++r) up[r] = r;
-    auto root = [&](int r) {
-        while (up[r] != r) {
-            up[r] = up[up[r]];
-            r = up[r];
-        }
-        return r;
-    };
-    for (int r = 0; r < S.n; ++r)
-        for (int d = 0; d < 6; ++d) {
-            const int c = nbr[(size_t)d * S.npad + r];
-            if (c < 0) continue;
-            const int a = root(r), b = root(c);
-            if (a != b) up[std::max(a, b)] = std::min(a, b);  // the root is the smallest row
-        }
-    const long long plane = (long long)S.cell_ny * S.cell_nz;
-    std::vector<char> open((size_t)S.n, 0);
-    for (int r = 0; r < S.n; ++r) {
-        const long long i = cell[r] / plane;
-        if (i == 0 || i == S.d0 - 1) open[root(r)] = 1;
-    }
-    std::vector<int> pins;
-    for (int r = 0; r < S.n; ++r)
-        if (root(r) == r && !open[r]) pins.push_back(r);
-    S.npins = (int)pins.size();
-    if (!pins.empty()) {
-        S.pins.alloc(pins.size(), st);
-        NS3D_CUDA_CHECK(cudaMemcpyAsync(S.pins.p, pins.data(), pins.size() * 4, cudaMemcpyHostToDevice, st));
-        NS3D_CUDA_CHECK(cudaStreamSynchronize(st));
-    }
-}
-
 template <int CAP>
 void MixedSetT<CAP>::configure(const std::vector<SolveItem> &items, cudaStream_t st) {
     std::vector<const double *> key;
@@ -166,7 +124,6 @@ void MixedSetT<CAP>::configure(const std::vector<SolveItem> &items, cudaStream_t
     for (int i = 0; i < ns; ++i) {
         DevSys &S = *items[i].sys;
         S.allocate_f32(st);
-        if (S.cell_ny > 0 && S.npins < 0) find_isolated_clusters(S, st);
         MSys &m = ms[i];
         std::memset(&m, 0, sizeof m);
         m.n = S.n;
@@ -243,7 +200,6 @@ void MixedSetT<CAP>::run(const std::vector<SolveItem> &items, cudaStream_t st, s
     for (int i = 0; i < ns; ++i) {
         DevSys &S = *items[i].sys;
         launch_to_f32(S.coef.p, S.invdiag.p, S.npad, S.coef32.p, S.invdiag32.p, st);
-        launch_pin_rows(S.coef32.p, S.invdiag32.p, S.npad, S.pins.p, S.npins, st);
         if (set_.sys[i].mg.nlev > 0) launch_mg_galerkin(set_.sys[i], st);
         DCState d;
         std::memset(&d, 0, sizeof d);

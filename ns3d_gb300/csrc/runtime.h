@@ -119,11 +119,6 @@ struct DevSys {
     // FP32 copy of the system and the FP32 Krylov vectors (mixed precision),
     // allocated on first use
     DBuf<float> coef32, invdiag32, fx, fr, fr0, fp, fv, fy, fs, fz, ft, fp2, fv2;
-    // pressure systems: one row of every isolated pore cluster (no cell on
-    // the inlet or outlet plane; its rows sum to zero, the block is
-    // singular), pinned in the FP32 copy; npins < 0 until found
-    DBuf<int> pins;
-    int npins = -1;
     void allocate(int rows, int first_extent, cudaStream_t st);
     void allocate_f32(cudaStream_t st);
     SysView view() const {

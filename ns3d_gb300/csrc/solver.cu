@@ -1058,6 +1058,7 @@ NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, 
 // the state a solve starts from: no result, initial relaxation, no history
 void ns3d_handle::begin_solve() {
     std::memset(&res, 0, sizeof res);
+    p_fp64 = false;
     su = sv = sw = sp = SolveOutcome();
     alpha = alpha0;
     beta = beta0;

@@ -127,11 +127,11 @@ def test_multilevel_with_isolated_pores_matches_fp64_oracle(gpulib, oracle, meth
 @pytest.mark.parametrize("method", ["SIMPLEC", "IDEAL"])
 def test_low_porosity_fibres_with_many_isolated_pores(gpulib, oracle, method, precision):
     """A fibre pack at porosity 0.4 holds about a hundred isolated pore
-    clusters of 2-14 cells.  Their singular blocks are pinned in the FP32
-    copy of the pressure systems (one row each); without that the FP32 inner
-    solves grew along the blocks' constant modes and broke down every outer
-    iteration (a 74^3 serving request stalled at 600 outer iterations with K
-    10% off).  Both mixed modes must converge to the FP64 oracle's K."""
+    clusters of 2-14 cells, whose pressure blocks are singular.  The FP32
+    inner solves can stall on such systems (a 74^3 serving request once
+    stalled at 600 outer iterations with K 10% off); a mixed pressure solve
+    that fails is redone in FP64 from its starting guess.  Both mixed modes
+    must converge to the FP64 oracle's K."""
     img, _ = synth.random_fibres((40, 36, 32), 2, 0.40, 81)
     kw = dict(method=method, maxitSIMPLE=600, simpletol=1e-6)
     g = solver(gpulib, img, params(gpulib, precision=precision, **kw))
