@@ -268,6 +268,11 @@ NS3D_API int ns3d_get_profile(ns3d_handle *h, ns3d_profile *out);
 /* kernels this library launched in the process so far (every handle,
  * server and batch call) */
 NS3D_API int64_t ns3d_kernel_launches(void);
+/* pressure(-correction) solves of the handle's last solve that ran in mixed
+ * precision, ended without success and were redone in FP64 (the precision
+ * then stays FP64 for that solve's later pressure systems); 0 for FP64
+ * handles, -1 for a NULL handle */
+NS3D_API int32_t ns3d_mixed_fallbacks(const ns3d_handle *h);
 
 /*
  * BiCGSTAB that allocates nothing.  No counterpart in the reference: it
@@ -394,16 +399,18 @@ NS3D_API int ns3d_server_set_merging(ns3d_server *s, int32_t lanes);
 NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out);
 /*
  * Lockstep solves (no counterpart in the reference, which solves one image
- * per process): the SIMPLEC solves (SIMPLECSOLVER::Solve, src/SIMPLEC.cxx:
- * 73-232) of n opened handles driven together by the calling thread.  Every
- * image takes exactly its own steps -- result, fields and logs are
- * bit-identical to ns3d_solve of that handle -- but each step runs for all
- * images at once: their kernels on one stream, each BiCGSTAB step as merged
- * sets (one persistent launch per round over the ragged chunk lists of all
- * images, by each image's precision), one host wait per read-back for all.
- * Every handle must use method SIMPLEC; status[i] (may be NULL) receives
- * each outcome.  The batch form opens, solves and closes n images (all of
- * them resident at once).
+ * per process): the solves of n opened handles, any mix of the four methods
+ * (SIMPLECSOLVER::Solve, src/SIMPLEC.cxx:73-232; SIMPLERSOLVER::Solve,
+ * src/SIMPLER.cxx:75-270; SIMPLERRSOLVER::Solve, src/SIMPLERR.cxx:75-280;
+ * IDEALSOLVER::Solve, src/IDEAL.cxx:75-281), driven together by the calling
+ * thread.  Every image takes exactly its own steps -- result, fields and
+ * logs are bit-identical to ns3d_solve of that handle -- but each stage of
+ * an outer iteration runs for all images at once: their kernels on one
+ * stream, each BiCGSTAB step as merged sets (one persistent launch per round
+ * over the ragged chunk lists of all images, by each image's precision), one
+ * host wait per read-back for all.  status[i] (may be NULL) receives each
+ * outcome.  The batch form opens, solves and closes n images (all of them
+ * resident at once).
  */
 NS3D_API int ns3d_solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status);
 NS3D_API int ns3d_batch_solve_lockstep(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,

@@ -94,6 +94,8 @@ def _declare(lib):
         sig["ns3d_get_profile"] = (C.c_int, [C.c_void_p, _P(Profile)])
     if hasattr(lib, "ns3d_kernel_launches"):
         sig["ns3d_kernel_launches"] = (C.c_int64, [])
+    if hasattr(lib, "ns3d_mixed_fallbacks"):
+        sig["ns3d_mixed_fallbacks"] = (C.c_int32, [C.c_void_p])
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
         f.restype = res
@@ -215,6 +217,10 @@ class Solver:
         r = Result()
         self._check(self.lib.ns3d_get_result(self.h, C.byref(r)))
         return r
+
+    def mixed_fallbacks(self):
+        """Mixed-precision pressure solves of the last solve redone in FP64."""
+        return self.lib.ns3d_mixed_fallbacks(self.h)
 
     def assemble_momentum(self):
         self._check(self.lib.ns3d_assemble_momentum(self.h))
@@ -483,8 +489,9 @@ def autotune_table(lib):
 
 
 def solve_lockstep(lib, solvers):
-    """ns3d_solve_lockstep: the SIMPLEC solves of `solvers` driven together by
-    this thread.  Returns (return code, per-solver statuses)."""
+    """ns3d_solve_lockstep: the solves of `solvers` (any mix of methods)
+    driven together by this thread.  Returns (return code, per-solver
+    statuses)."""
     lib = _declare_server(lib)
     n = len(solvers)
     hs = (C.c_void_p * n)(*[s.h.value for s in solvers])

@@ -89,7 +89,7 @@ struct ns3d_handle {
         run_fp64(kp, items, out);
         out[0].work += wasted;
     }
-    int p_fallbacks = 0;  // mixed pressure solves redone in FP64 (all solves of this handle)
+    int p_fallbacks = 0;  // mixed pressure solves redone in FP64 (reset by begin_solve)
 
     // physical constants and relaxation state (NavierStokesBase members)
     double dx, dy, dz, mu, rho, p0, p1, gradp, alpha0, beta0, alpha, beta;

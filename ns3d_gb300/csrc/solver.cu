@@ -879,6 +879,8 @@ NS3D_API int ns3d_debug_barrier_timeout(int32_t extra_arrivals, double limit_s) 
     return NS3D_OK;
 }
 
+NS3D_API int32_t ns3d_mixed_fallbacks(const ns3d_handle *h) { return h ? h->p_fallbacks : -1; }
+
 NS3D_API int ns3d_abi_version(void) { return NS3D_ABI_VERSION; }
 NS3D_API const char *ns3d_backend_name(void) { return "gb300"; }
 NS3D_API const char *ns3d_last_error(void) { return g_err.c_str(); }
@@ -1059,6 +1061,7 @@ NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, 
 void ns3d_handle::begin_solve() {
     std::memset(&res, 0, sizeof res);
     p_fp64 = false;
+    p_fallbacks = 0;
     su = sv = sw = sp = SolveOutcome();
     alpha = alpha0;
     beta = beta0;
@@ -1093,8 +1096,7 @@ static int solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status) {
     NS3D_TRY
     if (n < 0 || (n > 0 && !hs)) throw ApiError(NS3D_ERR_ARG, "ns3d_solve_lockstep: bad arguments");
     for (int i = 0; i < n; ++i) {
-        const ns3d_handle &h = *checked(hs[i]);
-        if (h.prm.method != NS3D_SIMPLEC) throw ApiError(NS3D_ERR_ARG, "lockstep solves run SIMPLEC only");
+        checked(hs[i]);
         for (int j = 0; j < i; ++j)
             if (hs[j] == hs[i]) throw ApiError(NS3D_ERR_ARG, "ns3d_solve_lockstep: a handle appears twice");
     }

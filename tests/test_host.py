@@ -49,7 +49,8 @@ def test_oracle_exports_the_solver_symbols(oracle):
                  "ns3d_group_get_stats", "ns3d_group_destroy", "ns3d_server_set_merging",
                  "ns3d_server_group_stats", "ns3d_batch_solve_merged", "ns3d_autotune_enable",
                  "ns3d_autotune_table", "ns3d_solve_lockstep", "ns3d_batch_solve_lockstep",
-                 "ns3d_debug_barrier_timeout", "ns3d_server_submit_resident", "ns3d_kernel_launches"}
+                 "ns3d_debug_barrier_timeout", "ns3d_server_submit_resident", "ns3d_kernel_launches",
+                 "ns3d_mixed_fallbacks"}
     for s in declared_symbols():
         if s not in host_only:
             assert hasattr(oracle, s), s
