@@ -642,19 +642,29 @@ def run_gpu(args):
 
 def run_case(args):
     """One solve of a named workload (ncu captures: a launch of the kernel of
-    interest on a known size): the 64^3 or 128^3 sphere pack, SIMPLEC,
-    `--max-outer` outer iterations, in the given precision."""
+    interest on a known size): the 64^3 or 128^3 sphere pack, SIMPLEC, or
+    request `--request` of the serving stream, `--max-outer` outer
+    iterations, in the given precision."""
     import ns3d_gb300
     from ns3d_gb300 import capi, synth, workloads
     lib = ns3d_gb300.lib()
-    img, info = {"sphere64": workloads.sphere64, "sphere128": workloads.sphere128}[args.case]()
     prec = {"fp64": 0, "mixed": 1, "mixed_mg": 2}[args.precision]
-    p = workloads.solve_params(capi, lib, img.shape[0], "SIMPLEC", 1, prec, max_outer=args.max_outer)
+    if args.case == "stream":
+        q = workloads.stream_request(args.request)
+        img, _, _ = capi.generate_image(lib, q["kind"], q["shape"], q["radius"], q["porosity"], q["image_seed"])
+        p = workloads.stream_params(capi, lib, q, prec, max_outer=args.max_outer)
+    else:
+        img, info = {"sphere64": workloads.sphere64, "sphere128": workloads.sphere128}[args.case]()
+        p = workloads.solve_params(capi, lib, img.shape[0], "SIMPLEC", 1, prec, max_outer=args.max_outer)
     s = capi.Solver(lib, p, synth.to_raw(img), img.shape)
+    l0 = lib.ns3d_kernel_launches()
     t = time.perf_counter()
     r = s.solve()
-    print(json.dumps({"case": args.case, "precision": args.precision, "np": s.sizes.np, "K": r.K,
-                      "outer_iterations": int(r.iterations), "seconds": time.perf_counter() - t}))
+    print(json.dumps({"case": args.case, "request": args.request if args.case == "stream" else None,
+                      "precision": args.precision, "np": s.sizes.np, "K": r.K,
+                      "outer_iterations": int(r.iterations), "krylov_iterations": int(r.krylov_iterations),
+                      "launches": int(lib.ns3d_kernel_launches() - l0), "fallbacks": s.mixed_fallbacks(),
+                      "seconds": time.perf_counter() - t}))
     s.close()
     return 0
 
@@ -681,8 +691,9 @@ def main():
     ap.add_argument("--batch64-images", type=int, default=64)
     ap.add_argument("--large", action="store_true", help="add the 256^3 fibre-pack sample (opt-in)")
     ap.add_argument("--large-outer", type=int, default=LARGE_OUTER)
-    ap.add_argument("--case", choices=["sphere64", "sphere128"],
+    ap.add_argument("--case", choices=["sphere64", "sphere128", "stream"],
                     help="profiling mode: one solve of this workload instead of the benchmark")
+    ap.add_argument("--request", type=int, default=13, help="the stream request of --case stream")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "mixed", "mixed_mg"])
     ap.add_argument("--max-outer", type=int, default=1)
     args = ap.parse_args()
