@@ -317,11 +317,30 @@ __device__ __forceinline__ float mg_spmv(const MGView &L, int row, const float *
     return acc;
 }
 
+// Jacobi sweeps on the coarsest level by the calling block: x = w D^-1 b,
+// then `sweeps` times t = b - A x, x += w D^-1 t
+__device__ void mg_coarsest(const MGView &L, float w, int sweeps) {
+    for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] = w * L.invdiag[r] * L.b[r];
+    __syncthreads();
+    for (int it = 0; it < sweeps; ++it) {
+        for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
+        __syncthreads();
+        for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] += w * L.invdiag[r] * L.t[r];
+        __syncthreads();
+    }
+}
+
 // x0 = M^-1 b0: one V-cycle -- a damped Jacobi sweep from zero, the residual
 // restricted to the next level (sum over the block), ... , Jacobi sweeps on
 // the coarsest level in block 0, then on the way up the correction of the
 // coarser level added and one damped Jacobi sweep.  Every thread of the grid
 // calls it (grid barriers between the passes); false when a barrier failed.
+// The fine level's Jacobi start x0 = w D^-1 b0 is already written by the
+// loop phase that computed b0 (p or s), so the V-cycle starts with the
+// fine residual.  (Fusing the Jacobi start, residual and restriction into
+// one pass per coarse row -- one grid barrier per level instead of three,
+// neighbours' starts recomputed -- gave the same values but measured 3-8%
+// slower, on the coarse levels as on the fine one.)
 __device__ bool mg_apply(const MSys &S, const float *b0, float *x0, GridBar *bar, unsigned int &target,
                          int *s_ok) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -330,12 +349,13 @@ __device__ bool mg_apply(const MSys &S, const float *b0, float *x0, GridBar *bar
     const float w = S.mg.omega;
     for (int k = 0; k < K; ++k) {
         const MGView L = mg_level(S, k, b0, x0);
-        const int lim = k == 0 ? L.npad : L.n;  // level 0: padding rows get finite values
-        for (int r = gtid; r < lim; r += gth) L.x[r] = w * L.invdiag[r] * L.b[r];
-        if (!grid_sync(bar, target, s_ok)) return false;
+        const MGLevel &C = S.mg.lev[k + 1];
+        if (k > 0) {
+            for (int r = gtid; r < L.n; r += gth) L.x[r] = w * L.invdiag[r] * L.b[r];
+            if (!grid_sync(bar, target, s_ok)) return false;
+        }
         for (int r = gtid; r < L.n; r += gth) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
         if (!grid_sync(bar, target, s_ok)) return false;
-        const MGLevel &C = S.mg.lev[k + 1];
         for (int I = gtid; I < C.n; I += gth) {
             float acc = 0.0f;
             for (int q = C.mstart[I]; q < C.mstart[I + 1]; ++q) acc += L.t[C.members[q]];
@@ -343,20 +363,8 @@ __device__ bool mg_apply(const MSys &S, const float *b0, float *x0, GridBar *bar
         }
         if (!grid_sync(bar, target, s_ok)) return false;
     }
-    {
-        const MGView L = mg_level(S, K, b0, x0);
-        if (blockIdx.x == 0) {
-            for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] = w * L.invdiag[r] * L.b[r];
-            __syncthreads();
-            for (int it = 0; it < S.mg.sweeps; ++it) {
-                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
-                __syncthreads();
-                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] += w * L.invdiag[r] * L.t[r];
-                __syncthreads();
-            }
-        }
-        if (!grid_sync(bar, target, s_ok)) return false;
-    }
+    if (blockIdx.x == 0) mg_coarsest(mg_level(S, K, b0, x0), w, S.mg.sweeps);
+    if (!grid_sync(bar, target, s_ok)) return false;
     for (int k = K - 1; k >= 0; --k) {
         const MGView L = mg_level(S, k, b0, x0);
         const MGLevel &C = S.mg.lev[k + 1];
@@ -411,13 +419,15 @@ __device__ bool mg_apply_set(const MSetArgT<CAP> &A, const KState *sst, const in
         if (on(q)) kmax = max(kmax, A.sys[q].mg.nlev);
     for (int k = 0; k < kmax; ++k) {
         auto part = [&](int q) { return on(q) && k < A.sys[q].mg.nlev; };
-        mg_rows(A, part, [&](int q) { return k == 0 ? A.sys[q].npad : A.sys[q].mg.lev[k].n; },
-                [&](int q, int r) {
-                    const MGView L = lvl(q, k);
-                    const float w = A.sys[q].mg.omega;
-                    L.x[r] = w * L.invdiag[r] * L.b[r];
-                });
-        if (!grid_sync(bar, target, s_ok)) return false;
+        if (k > 0) {  // the fine level's start is written by the loop phase
+            mg_rows(A, part, [&](int q) { return A.sys[q].mg.lev[k].n; },
+                    [&](int q, int r) {
+                        const MGView L = lvl(q, k);
+                        const float w = A.sys[q].mg.omega;
+                        L.x[r] = w * L.invdiag[r] * L.b[r];
+                    });
+            if (!grid_sync(bar, target, s_ok)) return false;
+        }
         mg_rows(A, part, [&](int q) { return k == 0 ? A.sys[q].n : A.sys[q].mg.lev[k].n; },
                 [&](int q, int r) {
                     const MGView L = lvl(q, k);
@@ -439,16 +449,7 @@ __device__ bool mg_apply_set(const MSetArgT<CAP> &A, const KState *sst, const in
         for (int q = 0; q < A.nsys; ++q) {
             if (!on(q)) continue;
             if (j++ % gridDim.x != blockIdx.x) continue;
-            const MGView L = lvl(q, A.sys[q].mg.nlev);
-            const float w = A.sys[q].mg.omega;
-            for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] = w * L.invdiag[r] * L.b[r];
-            __syncthreads();
-            for (int it = 0; it < A.sys[q].mg.sweeps; ++it) {
-                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.t[r] = L.b[r] - mg_spmv(L, r, L.x);
-                __syncthreads();
-                for (int r = threadIdx.x; r < L.n; r += blockDim.x) L.x[r] += w * L.invdiag[r] * L.t[r];
-                __syncthreads();
-            }
+            mg_coarsest(lvl(q, A.sys[q].mg.nlev), A.sys[q].mg.omega, A.sys[q].mg.sweeps);
         }
         if (!grid_sync(bar, target, s_ok)) return false;
     }
@@ -707,7 +708,8 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     const int row = r0 + m * LANES;
                     const float p = __fmaf_rn(beta, __fmaf_rn(-w, S.v[row], S.p[row]), S.r[row]);
                     S.p[row] = p;
-                    S.y[row] = S.invdiag32[row] * p;
+                    // a system with a hierarchy: the V-cycle's start w D^-1 p
+                    S.y[row] = S.mg.nlev > 0 ? S.mg.omega * S.invdiag32[row] * p : S.invdiag32[row] * p;
                 }
             }
             if (!grid_sync(bar, target, &s_ok)) break;
@@ -751,7 +753,7 @@ __global__ void __launch_bounds__(LOOP_THREADS, LOOP_MIN_BLOCKS)
                     const int row = r0 + m * LANES;
                     const float sv = __fmaf_rn(-alpha, S.v[row], S.r[row]);
                     S.s[row] = sv;
-                    S.z[row] = S.invdiag32[row] * sv;
+                    S.z[row] = S.mg.nlev > 0 ? S.mg.omega * S.invdiag32[row] * sv : S.invdiag32[row] * sv;
                 }
             }
             if (!grid_sync(bar, target, &s_ok)) break;
