@@ -64,6 +64,8 @@ def _first_diff(a, b):
 def test_records_present():
     names = {os.path.basename(p) for p in RECORDS}
     assert "oracle_sphere64_SIMPLEC.json" in names
+    for method in ("SIMPLEC", "SIMPLER", "SIMPLERR", "IDEAL"):
+        assert "oracle_sphere128_%s.json" % method in names, method
 
 
 @pytest.mark.parametrize("path", RECORDS, ids=[os.path.basename(p)[7:-5] for p in RECORDS])
