@@ -409,8 +409,10 @@ NS3D_API int ns3d_server_group_stats(ns3d_server *s, ns3d_group_stats *out);
  * stream, each BiCGSTAB step as merged sets (one persistent launch per round
  * over the ragged chunk lists of all images, by each image's precision), one
  * host wait per read-back for all.  status[i] (may be NULL) receives each
- * outcome.  The batch form opens, solves and closes n images (all of them
- * resident at once).
+ * outcome.  A handle attached to a solve group (ns3d_set_group) takes part
+ * like any other: its BiCGSTAB steps join the lockstep call's merged sets,
+ * not the group's.  The batch form opens, solves and closes n images (all of
+ * them resident at once).
  */
 NS3D_API int ns3d_solve_lockstep(ns3d_handle *const *hs, int32_t n, int32_t *status);
 NS3D_API int ns3d_batch_solve_lockstep(const ns3d_params *params, const uint8_t *const *raws, const int32_t *dims,
