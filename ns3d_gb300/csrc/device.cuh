@@ -138,6 +138,14 @@ using KSetArgMerged = KSetArgT<KMAX_MERGED>;
 static_assert(sizeof(KSetArgMerged) <= 32000, "kernel parameter space");
 
 // The persistent BiCGSTAB loop kernel: block shape and its grid barrier.
+// Loads of global data that no thread writes during the kernel (matrix
+// coefficients, neighbour tables, the multilevel hierarchy) go through the
+// read-only data path (measured 0.6% faster in the FP64 loop, 1.3% in the
+// FP32 multilevel loop); never for shared memory or for vectors the kernel
+// itself updates.
+template <class T>
+__device__ __forceinline__ T ro(const T *p) { return __ldg(p); }
+
 #ifndef NS3D_LOOP_THREADS
 #define NS3D_LOOP_THREADS 1024
 #endif

@@ -69,8 +69,8 @@ __device__ __forceinline__ double spmv_row_nb(const KSys &S, int row, const doub
     const double xP = x[row];
     const double xW = x[nW >= 0 ? nW : row], xE = x[nE >= 0 ? nE : row], xS = x[nS >= 0 ? nS : row];
     const double xN = x[nN >= 0 ? nN : row], xB = x[nB >= 0 ? nB : row], xT = x[nT >= 0 ? nT : row];
-    const double cP = cf[0], cW = cf[1 * np], cE = cf[2 * np], cS = cf[3 * np], cN = cf[4 * np],
-                 cB = cf[5 * np], cT = cf[6 * np];
+    const double cP = ro(cf), cW = ro(cf + 1 * np), cE = ro(cf + 2 * np), cS = ro(cf + 3 * np),
+                 cN = ro(cf + 4 * np), cB = ro(cf + 5 * np), cT = ro(cf + 6 * np);
     const bool wlate = nW >= 0 && nW == row - 1;
     const bool eearly = nE >= 0 && nE == row + 1;
     double acc = 0.0;

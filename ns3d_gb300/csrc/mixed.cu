@@ -48,14 +48,15 @@ __device__ __forceinline__ float spmv_f32_row(const MSys &S, int row, const floa
     const size_t np = (size_t)S.npad;
     const int *nb = S.nbr + row;
     const float *cf = S.coef32 + row;
-    const int nW = nb[0 * np], nE = nb[1 * np], nS = nb[2 * np], nN = nb[3 * np], nB = nb[4 * np], nT = nb[5 * np];
-    float acc = cf[0] * x[row];
-    acc = __fmaf_rn(cf[1 * np], x[nW >= 0 ? nW : row], acc);
-    acc = __fmaf_rn(cf[3 * np], x[nS >= 0 ? nS : row], acc);
-    acc = __fmaf_rn(cf[5 * np], x[nB >= 0 ? nB : row], acc);
-    acc = __fmaf_rn(cf[6 * np], x[nT >= 0 ? nT : row], acc);
-    acc = __fmaf_rn(cf[4 * np], x[nN >= 0 ? nN : row], acc);
-    acc = __fmaf_rn(cf[2 * np], x[nE >= 0 ? nE : row], acc);
+    const int nW = ro(nb + 0 * np), nE = ro(nb + 1 * np), nS = ro(nb + 2 * np), nN = ro(nb + 3 * np),
+              nB = ro(nb + 4 * np), nT = ro(nb + 5 * np);
+    float acc = ro(cf) * x[row];
+    acc = __fmaf_rn(ro(cf + 1 * np), x[nW >= 0 ? nW : row], acc);
+    acc = __fmaf_rn(ro(cf + 3 * np), x[nS >= 0 ? nS : row], acc);
+    acc = __fmaf_rn(ro(cf + 5 * np), x[nB >= 0 ? nB : row], acc);
+    acc = __fmaf_rn(ro(cf + 6 * np), x[nT >= 0 ? nT : row], acc);
+    acc = __fmaf_rn(ro(cf + 4 * np), x[nN >= 0 ? nN : row], acc);
+    acc = __fmaf_rn(ro(cf + 2 * np), x[nE >= 0 ? nE : row], acc);
     return acc;
 }
 
@@ -308,11 +309,11 @@ __device__ __forceinline__ float mg_spmv(const MGView &L, int row, const float *
     const size_t np = (size_t)L.npad;
     const int *nb = L.nbr + row;
     const float *cf = L.coef + row;
-    float acc = cf[0] * x[row];
+    float acc = ro(cf) * x[row];
 #pragma unroll
     for (int d = 0; d < 6; ++d) {
-        const int c = nb[d * np];
-        acc = __fmaf_rn(cf[(d + 1) * np], x[c >= 0 ? c : row], acc);
+        const int c = ro(nb + d * np);
+        acc = __fmaf_rn(ro(cf + (d + 1) * np), x[c >= 0 ? c : row], acc);
     }
     return acc;
 }
