@@ -39,6 +39,20 @@ def test_gpu_library_exports_every_declared_symbol(gpulib):
     assert gpulib.ns3d_abi_version() == 1
 
 
+def test_gpu_library_exports_nothing_undeclared(gpulib):
+    """The C-ABI is exactly the header: no ns3d_ function leaves the library
+    undeclared (everything else is hidden)."""
+    import shutil
+    import subprocess
+    import ns3d_gb300
+    if not shutil.which("nm"):
+        pytest.skip("nm not available")
+    out = subprocess.run(["nm", "-D", "--defined-only", ns3d_gb300.LIB_PATH], capture_output=True, text=True,
+                         check=True).stdout
+    exported = {l.split()[-1] for l in out.splitlines() if " T " in l}
+    assert exported == set(declared_symbols())
+
+
 def test_oracle_exports_the_solver_symbols(oracle):
     host_only = {"ns3d_ini_read", "ns3d_vti_read_u8", "ns3d_vti_read_f64", "ns3d_vti_write_f64",
                  "ns3d_vti_write_u8", "ns3d_run_ini", "ns3d_bicgstab_noalloc", "ns3d_noalloc_last_error",
