@@ -368,7 +368,13 @@ s = capi.Solver(lib, p, synth.to_raw(img), img.shape)
 t = time.perf_counter()
 r = s.solve()
 dt = time.perf_counter() - t
-print(json.dumps({"seconds": dt, "K": r.K, "outer_iterations": int(r.iterations), "converged": int(r.converged)}))
+rec = {"seconds": dt, "K": r.K, "outer_iterations": int(r.iterations), "converged": int(r.converged)}
+import ctypes as C
+ph = (C.c_double * 4)()
+if lib.ns3d_oracle_phase_seconds(ph) == 0:
+    rec["phase_seconds"] = {"assembly": ph[0], "bicgstab": ph[1], "corrections": ph[2], "diagnostics": ph[3],
+                            "other": dt - sum(ph)}
+print(json.dumps(rec))
 """
 
 

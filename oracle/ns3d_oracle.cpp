@@ -138,6 +138,20 @@ double det_dot(const std::vector<double> &a, const std::vector<double> &b, long 
  * They exist to measure how much a solve's trajectory depends on rounding
  * alone (the reference's Eigen reduction order cannot be reproduced).
  */
+// Wall time per phase of the solves since the last ns3d_solve started (the
+// CPU baseline reports it beside the total): 0 assembly (momentum, right-hand
+// sides, pseudo-velocities, pressure systems), 1 BiCGSTAB solves,
+// 2 corrections, 3 diagnostics (permeability, divergence).
+double g_phase_s[4] = {0, 0, 0, 0};
+struct PhaseTimer {
+    int slot;
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    explicit PhaseTimer(int s) : slot(s) {}
+    ~PhaseTimer() {
+        g_phase_s[slot] += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
 int g_arith = 0;
 
 void read_arith_mode() {
@@ -274,6 +288,7 @@ struct SolveOut {
  */
 SolveOut bicgstab(const System &A, const std::vector<double> &b, std::vector<double> &x,
                   double tol, long maxit, long *krylov_rows) {
+    PhaseTimer phase_timer(1);
     const long n = A.n;
     SolveOut out;
     out.valid = true;
@@ -949,6 +964,7 @@ void assemble_mom_z(Handle &h, const std::vector<double> &uc, const std::vector<
 /* AssembleAllMomentum + the Jacobi "factorization", src/NSBase.cxx:853-884 */
 void assemble_all_momentum(Handle &h, const std::vector<double> &uc, const std::vector<double> &vc,
                            const std::vector<double> &wc) {
+    PhaseTimer phase_timer(0);
     assemble_mom_x(h, uc, vc, wc);
     h.U.compute_invdiag();
     h.U.compute_rowsum();
@@ -964,6 +980,7 @@ void assemble_all_momentum(Handle &h, const std::vector<double> &uc, const std::
 
 /* ---- momentum right-hand sides, src/NSBase.cxx:1445-1546 ---------------- */
 void rhs_u(Handle &h) {
+    PhaseTimer phase_timer(0);
     System &A = h.U;
     const double idx = 1 / h.dx;
     const int nx = h.nx;
@@ -980,6 +997,7 @@ void rhs_u(Handle &h) {
     }
 }
 void rhs_v(Handle &h) {
+    PhaseTimer phase_timer(0);
     System &A = h.V;
     const double idy = 1 / h.dy;
 #pragma omp parallel for schedule(static)
@@ -991,6 +1009,7 @@ void rhs_v(Handle &h) {
     }
 }
 void rhs_w(Handle &h) {
+    PhaseTimer phase_timer(0);
     System &A = h.W;
     const double idz = 1 / h.dz;
 #pragma omp parallel for schedule(static)
@@ -1006,6 +1025,7 @@ void rhs_w(Handle &h) {
 /* order of the off-diagonal products: E, W, N, S, T, B */
 void compute_hat(const Handle &h, const System &A, const std::vector<double> &xc, const std::vector<double> &xold,
                  std::vector<double> &hat) {
+    PhaseTimer phase_timer(0);
     hat.assign((size_t)A.n, 0.0);
     const int order[6] = {SE, SW, SN, SS, ST, SB};
 #pragma omp parallel for schedule(static)
@@ -1025,6 +1045,7 @@ void compute_hat(const Handle &h, const System &A, const std::vector<double> &xc
  * SIMPLEC (row sums), mode 2: pressure correction SIMPLE (a_P) */
 void assemble_pressure_system(Handle &h, int mode, bool relax, const std::vector<double> &uc,
                               const std::vector<double> &vc, const std::vector<double> &wc) {
+    PhaseTimer phase_timer(0);
     System &S = h.P;
     const int nx = h.nx, ny = h.ny, nz = h.nz;
     const double dx2 = h.dx * h.dx, dy2 = h.dy * h.dy, dz2 = h.dz * h.dz;
@@ -1100,6 +1121,7 @@ inline double clampdv(double d, double m) {
 }
 /* simplec=1 uses row sums, 0 uses the diagonal */
 void correct_velocity_simple(Handle &h, bool simplec, double dvmax) {
+    PhaseTimer phase_timer(2);
     const int nx = h.nx, ny = h.ny, nz = h.nz;
     (void)ny;
     const std::vector<double> &au = simplec ? h.U.rowsum : h.U.c[SP];
@@ -1139,6 +1161,7 @@ void correct_velocity_simpler(Handle &h, const std::vector<double> &pp, std::vec
                               std::vector<double> &vc, std::vector<double> &wc, const std::vector<double> &uh,
                               const std::vector<double> &vh, const std::vector<double> &wh, double p_0,
                               double p_1) {
+    PhaseTimer phase_timer(2);
     const int nx = h.nx;
     const std::vector<double> &au = h.U.c[SP], &av = h.V.c[SP], &aw = h.W.c[SP];
 #pragma omp parallel for schedule(static)
@@ -1239,6 +1262,7 @@ void compute_pressure_field(Handle &h) {
 
 /* CorrectPressureField, src/NSBase.cxx:2367-2380 */
 void correct_pressure_field(Handle &h) {
+    PhaseTimer phase_timer(2);
     double mx = -HUGE_VAL, mn = HUGE_VAL;
     for (int r = 0; r < h.np; ++r) {
         double x = h.pc[(size_t)r];
@@ -1263,6 +1287,7 @@ void correct_pressure_field(Handle &h) {
 
 /* ---- diagnostics: src/NSBase.cxx:1886-2080 ------------------------------ */
 void compute_permeability(Handle &h, double &Q, double &v_moy, double &K) {
+    PhaseTimer phase_timer(3);
     const int nx = h.nx, ny = h.ny, nz = h.nz, b = h.border;
     const double sx = h.dy * h.dz;
     const long plane = (long)ny * nz;
@@ -1308,6 +1333,7 @@ void compute_permeability(Handle &h, double &Q, double &v_moy, double &K) {
 }
 
 void compute_div(Handle &h, double &MaxDeltaV, double &normdiv, double &velocityNorm, double &maxdiv) {
+    PhaseTimer phase_timer(3);
     const int nx = h.nx, ny = h.ny, nz = h.nz;
     const double idx = 1 / h.dx, idy = 1 / h.dy, idz = 1 / h.dz;
     std::vector<double> dv((size_t)h.np), vel((size_t)h.np), dV((size_t)h.np);
@@ -1835,6 +1861,15 @@ NS3D_API int ns3d_set_output(ns3d_handle *H, const char *dir, const char *stem, 
     return NS3D_OK;
 }
 
+/* Oracle only (not in the header): wall seconds of the last ns3d_solve per
+ * phase -- out[0] assembly, out[1] BiCGSTAB solves, out[2] corrections,
+ * out[3] diagnostics. */
+NS3D_API int ns3d_oracle_phase_seconds(double *out) {
+    if (!out) return fail(NS3D_ERR_ARG, "NULL output");
+    for (int i = 0; i < 4; ++i) out[i] = g_phase_s[i];
+    return NS3D_OK;
+}
+
 NS3D_API int ns3d_solve(ns3d_handle *H) {
     if (!H) return fail(NS3D_ERR_ARG, "NULL handle");
     Handle &h = H->h;
@@ -1844,6 +1879,7 @@ NS3D_API int ns3d_solve(ns3d_handle *H) {
     h.beta = h.beta0;
     h.avgRMR.clear();
     h.RMR = h.old_RMR = 0;
+    for (double &t : g_phase_s) t = 0.0;
     switch (h.prm.method) {
         case NS3D_SIMPLEC: run_simplec(h); break;
         case NS3D_SIMPLER:

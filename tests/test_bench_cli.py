@@ -21,3 +21,22 @@ def test_reference_arm_prints_one_unavailable_line():
     assert rec["impl"] == "reference" and rec["unavailable"]
     assert rec["metric"].startswith("permeability solves/sec")
     assert "5 complete solves" in rec["unavailable"]
+
+
+def test_oracle_reports_phase_times(oracle):
+    """The CPU baseline's per-phase wall times (assembly, BiCGSTAB,
+    corrections, diagnostics) cover the solve and are reset by each solve."""
+    import ctypes as C
+    import time
+    from helpers import params, solver
+    from ns3d_gb300 import synth
+    img, _ = synth.rsa_spheres((16, 12, 14), 2, 0.6, seed=5)
+    s = solver(oracle, img, params(oracle, method="IDEAL", maxitSIMPLE=20))
+    for _ in range(2):
+        t = time.perf_counter()
+        s.solve()
+        dt = time.perf_counter() - t
+        ph = (C.c_double * 4)()
+        assert oracle.ns3d_oracle_phase_seconds(ph) == 0
+        assert all(x > 0 for x in ph) and sum(ph) <= dt
+    s.close()
