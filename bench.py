@@ -371,7 +371,7 @@ dt = time.perf_counter() - t
 rec = {"seconds": dt, "K": r.K, "outer_iterations": int(r.iterations), "converged": int(r.converged)}
 import ctypes as C
 ph = (C.c_double * 4)()
-if lib.ns3d_oracle_phase_seconds(ph) == 0:
+if hasattr(lib, "ns3d_oracle_phase_seconds") and lib.ns3d_oracle_phase_seconds(ph) == 0:
     rec["phase_seconds"] = {"assembly": ph[0], "bicgstab": ph[1], "corrections": ph[2], "diagnostics": ph[3],
                             "other": dt - sum(ph)}
 print(json.dumps(rec))
