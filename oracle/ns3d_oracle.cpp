@@ -138,10 +138,11 @@ double det_dot(const std::vector<double> &a, const std::vector<double> &b, long 
  * They exist to measure how much a solve's trajectory depends on rounding
  * alone (the reference's Eigen reduction order cannot be reproduced).
  */
-// Wall time per phase of the solves since the last ns3d_solve started (the
-// CPU baseline reports it beside the total): 0 assembly (momentum, right-hand
-// sides, pseudo-velocities, pressure systems), 1 BiCGSTAB solves,
-// 2 corrections, 3 diagnostics (permeability, divergence).
+// Wall time per phase since the last ns3d_solve started, process-wide (the
+// CPU baseline runs one solve per process and reports it beside the total):
+// 0 assembly (momentum, right-hand sides, pseudo-velocities, pressure
+// systems), 1 BiCGSTAB solves, 2 corrections, 3 diagnostics (permeability,
+// divergence).
 double g_phase_s[4] = {0, 0, 0, 0};
 struct PhaseTimer {
     int slot;
